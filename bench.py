@@ -1,0 +1,415 @@
+#!/usr/bin/env python
+"""HMC link-updates/s at 32^4 on GB300: mixed FP32/FP64 (headline) and plain FP64.
+
+One bench step is one full HMC trajectory of HybridMonteCarloDiagnostic on
+LatticeStateDefault<4>: momentum refresh N(0, 0.5/beta) on the device, Gauss projection,
+20 leap-frog steps of dt = 0.005, both Hamiltonians and the accept/reject -- D = 4, 32^4
+sites, beta = 2.0, size 1000, links from random_su3 drawn on the device (seed 1).
+value = links * md_steps * trajectories / device time of the timed trajectories.
+
+--impl reference times the CPU oracle (a C++ restatement of the reference's
+SymplecticEulerRayon + HybridMonteCarloDiagnostic, OpenMP over all host threads) on a
+bounded sample of the same workload: the same trajectory on an 8^4 sublattice.
+Under torchrun every rank runs an independent replica on its own GPU ("replicas only").
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "lattice-qcd-rs_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "HMC link-updates/s at 32^4: mixed FP32/FP64 vs plain FP64 GPU at equal plaquette error"
+UNIT = "link-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dim", type=int, default=4)
+    ap.add_argument("--L", type=int, default=32)
+    ap.add_argument("--beta", type=float, default=2.0)
+    ap.add_argument("--dt", type=float, default=0.005)
+    ap.add_argument("--md-steps", type=int, default=20)
+    ap.add_argument("--size", type=float, default=1000.0)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "f64"])
+    ap.add_argument("--fp64-steps", type=int, default=2, help="timed FP64 trajectories for the comparison leg")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample-L", type=int, default=8)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm_sorted = sorted(sm)
+        return {"sm_mhz": sm_sorted[len(sm_sorted) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "power_w_max": max(power), "samples": len(sm)}
+
+
+def smi_index():
+    """nvidia-smi index of this process's GPU (CUDA_VISIBLE_DEVICES when it is a plain index)."""
+    v = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0].strip()
+    return int(v) if v.isdigit() else 0
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle)
+def cpu_trajectory_rate(dim, L, beta, dt, md_steps, size, seconds, min_traj=2):
+    """Times full oracle trajectories (refresh on the host + projection + MD + accept)."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    rng = O.Rng(1)
+    links = O.links_random(dim, L, rng)
+    n_links = L ** dim * dim
+    # one untimed trajectory (warm-up)
+    e_raw = O.efield_normal(dim, L, rng, 0.5 / beta)
+    links = O.hmc_trajectory(dim, L, size, beta, links, e_raw, dt, md_steps, rng.uniform(0, 1))["links"]
+    t_total, n = 0.0, 0
+    while n < min_traj or t_total < seconds:
+        t0 = time.perf_counter()
+        e_raw = O.efield_normal(dim, L, rng, 0.5 / beta)
+        r = O.hmc_trajectory(dim, L, size, beta, links, e_raw, dt, md_steps, rng.uniform(0, 1))
+        t_total += time.perf_counter() - t0
+        links = r["links"]
+        n += 1
+        if n >= 50:
+            break
+    return n_links * md_steps * n / t_total, threads, n, t_total
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    dim, L = args.dim, args.cpu_sample_L
+    rng = O.Rng(1)
+    links = O.links_random(dim, L, rng)
+    n_links = L ** dim * dim
+
+    def one():
+        e_raw = O.efield_normal(dim, L, rng, 0.5 / args.beta)
+        return O.hmc_trajectory(dim, L, args.size, args.beta, links, e_raw, args.dt, args.md_steps,
+                                rng.uniform(0, 1))["links"]
+
+    for _ in range(args.warmup):
+        links = one()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        links = one()
+    elapsed = time.perf_counter() - t0
+    value = n_links * args.md_steps * args.steps / elapsed
+    sample = ("full HMC trajectories (host momentum draw, Gauss projection, %d leap-frog steps, both Hamiltonians, "
+              "accept) on a %d^%d sublattice of the %d^%d workload, beta %g, dt %g" %
+              (args.md_steps, L, dim, args.L, dim, args.beta, args.dt))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "HMC trajectory D=%d %d^%d (CPU sample %d^%d), beta %g, %d leap-frog steps dt %g, "
+                               "size %g" % (dim, args.L, dim, L, dim, args.beta, args.md_steps, args.dt, args.size),
+                   "implementation": "CPU oracle: C++ restatement of SymplecticEulerRayon + "
+                                     "HybridMonteCarloDiagnostic (the Rust reference cannot be built here)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+def algorithmic_md_bytes(n_links, md_steps, real_bytes):
+    """Bytes moved by the fused MD kernels of one trajectory at ideal neighbour reuse.
+    kick+drift launch: read U (18 reals) + E (8) + write E (8) + U' (18) = 52 reals per link;
+    final kick-only launch: read U (18) + E (8) + write E (8) = 34 reals per link."""
+    return n_links * real_bytes * (52 * md_steps + 34)
+
+
+def run_ours(args):
+    rank, world, local_rank = dist_env()
+    if world > 1:
+        # one GPU per replica: make the rank's GPU device 0 before CUDA initialises
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+    import numpy as np
+    import torch
+
+    import lqgpu
+
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream(device=dev)
+
+    dim, L, beta, dt, nmd, size = args.dim, args.L, args.beta, args.dt, args.md_steps, args.size
+    n_links = L ** dim * dim
+    prec = lqgpu.PRECISION_MIXED if args.precision == "mixed" else lqgpu.PRECISION_F64
+    real_bytes = 4 if prec == lqgpu.PRECISION_MIXED else 8
+    uni = np.random.default_rng(1000 + rank)
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    def max_over_ranks(x):
+        if pg is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x):
+        if pg is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def timed_trajectories(state, k_warm, k_timed, seed, sample_clocks=False):
+        results = []
+        for k in range(k_warm):
+            state.hmc_trajectory(dt, nmd, seed, 10_000 + k, float(uni.uniform()))
+        state.profile_read(reset=True)
+        sampler = ClockSampler(smi_index()) if sample_clocks else None
+        if sampler:
+            sampler.start()
+            time.sleep(0.5)
+        barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        for k in range(k_timed):
+            results.append(state.hmc_trajectory(dt, nmd, seed, k, float(uni.uniform())))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        barrier()
+        clocks = sampler.stop() if sampler else None
+        ms = ev0.elapsed_time(ev1)
+        prof = state.profile_read(reset=True)
+        return ms, wall, prof, results, clocks
+
+    # ---- headline precision
+    s = lqgpu.State(dim, L, size, beta, prec)
+    s.set_stream(stream.cuda_stream)
+    s.set_links_random(1 + rank)
+    s.profile_enable(True)
+    ms, wall, prof, res, clocks = timed_trajectories(s, args.warmup, args.steps, 77 + rank, sample_clocks=True)
+    ms_max = max_over_ranks(ms)
+    value = sum_over_ranks(n_links * nmd * args.steps) / (ms_max / 1000.0)
+    launches = sum(v[0] for v in prof.values())
+    md_launches, md_ms = prof["md"]
+    md_bytes = algorithmic_md_bytes(n_links, nmd, real_bytes) * args.steps
+    peak, peak_kind = measured_peaks()
+    achieved = md_bytes / (md_ms / 1000.0) / 1e9 if md_ms > 0 else 0.0
+    gauss_steps = [r["gauss_steps"] for r in res]
+    acc_rate = sum(r["accepted"] for r in res) / max(1, len(res))
+
+    # ---- e2e: momenta from pinned host memory through the C ABI test-mode entry, results back
+    e2e = None
+    if args.e2e_steps > 0:
+        shape = (L ** dim, dim, 8)
+        host_bufs = []
+        for j in range(2):
+            t = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+            t.normal_(0.0, 0.5 / beta, generator=torch.Generator().manual_seed(5 + j))
+            host_bufs.append(t.numpy())
+        s.hmc_refresh_upload(host_bufs[0])  # warm the staging buffer
+        s.hmc_propose(dt, nmd)
+        s.hmc_decide(True)
+        barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        d2h = 0
+        for k in range(args.e2e_steps):
+            steps = s.hmc_refresh_upload(host_bufs[k % 2])
+            p, h0, h1 = s.hmc_propose(dt, nmd)
+            s.hmc_decide(p >= 1.0 or float(uni.uniform()) < p)
+            plaq = s.average_trace_plaquette()
+            # residual reads of the projection (one double per check) + 8 doubles (proposal) + 3 (plaquette)
+            d2h += 8 * ((steps - 1) // 4 + 1) + 8 * 8 + 8 * 3
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = max_over_ranks(ev0.elapsed_time(ev1))
+        e2e = {"value": sum_over_ranks(n_links * nmd * args.e2e_steps) / (e2e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": int(np.prod(shape) * 8), "d2h_bytes_per_step": int(d2h / args.e2e_steps),
+               "path": "lq_hmc_refresh_upload + lq_hmc_propose + lq_hmc_decide + lq_average_trace_plaquette, "
+                       "momenta (f64, reference layout) from pinned host memory each trajectory"}
+    plaq_mixed = s.average_trace_plaquette()
+    s.close()
+
+    # ---- FP64 leg (the plain GPU form) and accuracy at equal inputs
+    fp64 = None
+    accuracy = None
+    if prec == lqgpu.PRECISION_MIXED and args.fp64_steps > 0:
+        s64 = lqgpu.State(dim, L, size, beta, lqgpu.PRECISION_F64)
+        s64.set_stream(stream.cuda_stream)
+        s64.set_links_random(1 + rank)
+        s64.profile_enable(True)
+        ms64, _, prof64, res64, _ = timed_trajectories(s64, 1, args.fp64_steps, 77 + rank)
+        ms64 = max_over_ranks(ms64)
+        v64 = sum_over_ranks(n_links * nmd * args.fp64_steps) / (ms64 / 1000.0)
+        md64_n, md64_ms = prof64["md"]
+        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.fp64_steps,
+                "mixed_over_fp64": value / v64,
+                "md_kernel_ms": md64_ms / max(1, md64_n),
+                "gauss_steps": [r["gauss_steps"] for r in res64]}
+        if not args.no_accuracy:
+            # identical momenta (host draw) and uniforms into both precisions, from identical links
+            sm = lqgpu.State(dim, L, size, beta, lqgpu.PRECISION_MIXED)
+            sm.set_links_random(5)
+            s64.set_links_random(5)
+            rngacc = np.random.default_rng(9)
+            errs_dh, errs_pl, dhs = [], [], []
+            for k in range(2):
+                e_raw = rngacc.normal(0.0, 0.5 / beta, size=(L ** dim, dim, 8))
+                u = float(rngacc.uniform())
+                out = []
+                for st in (s64, sm):
+                    st.hmc_refresh_upload(e_raw)
+                    p, h0, h1 = st.hmc_propose(dt, nmd)
+                    st.hmc_decide(p >= 1.0 or u < p)
+                    out.append((h1 - h0, st.average_trace_plaquette().real / 3.0))
+                errs_dh.append(abs(out[0][0] - out[1][0]))
+                errs_pl.append(abs(out[0][1] - out[1][1]))
+                dhs.append(out[0][0])
+            accuracy = {"trajectories": 2, "max_abs_delta_h_error": max(errs_dh),
+                        "max_abs_plaquette_error": max(errs_pl), "fp64_delta_h": dhs,
+                        "note": "mixed vs FP64 GPU from identical links, momenta and uniforms"}
+            sm.close()
+        s64.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, threads, n, t = cpu_trajectory_rate(dim, args.cpu_sample_L, beta, dt, nmd, size, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d full HMC trajectories (%d leap-frog steps, host momentum draw, Gauss projection, both "
+                         "Hamiltonians) on a %d^%d sublattice, %.1f s, OpenMP over all host threads" %
+                         (n, nmd, args.cpu_sample_L, dim, t)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if prec == lqgpu.PRECISION_MIXED else "f64", "data": "synthetic",
+            "config": {"workload": "HMC trajectory D=%d %d^%d, beta %g, %d leap-frog steps dt %g, size %g, "
+                                   "random_su3 start, device momenta N(0,0.5/beta) + Gauss projection"
+                                   % (dim, L, dim, beta, nmd, dt, size),
+                       "precision": args.precision, "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (links %.0f MB)" % (n_links * 18 * real_bytes / 1e6)},
+            "roofline": {"bound": "hbm", "kernel": "k_md (fused force + kick + drift)", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": None, "algorithmic_bytes_per_link": 52 * real_bytes,
+                         "md_launch_ms": md_ms / max(1, md_launches)},
+            "kernel_ms": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+            "gpu_launches": launches,
+            "gauss_steps": gauss_steps, "acceptance": acc_rate, "plaquette": plaq_mixed.real / 3.0,
+            "wall_ms_per_step": 1000.0 * wall / args.steps,
+            "clocks": clocks, "e2e": e2e, "fp64": fp64, "accuracy": accuracy, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

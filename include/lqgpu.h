@@ -1,0 +1,200 @@
+/*
+ * lqgpu.h -- C ABI of the GB300 (sm_103a) HMC molecular-dynamics library.
+ *
+ * A device-resident replacement for the hot path of lattice-qcd-rs v0.2.1: the state
+ * types LatticeStateDefault<D> / LatticeStateEFSyncDefault<LatticeStateDefault<D>, D>,
+ * the SymplecticIntegrator SymplecticEulerRayon, and the per-trajectory work of
+ * HybridMonteCarloDiagnostic.  Each entry point names the reference item it replaces
+ * (paths relative to the reference crate root).
+ *
+ * Conventions
+ *  - Every function returns an int32 status: LQ_OK (0) or one of the LQ_ERR_* codes.
+ *    No C++ exception crosses this boundary; nothing traps on the device.
+ *  - A handle is used by one host thread at a time (externally synchronised).
+ *  - All device work of a handle runs on the handle's CUDA stream (lq_state_set_stream).
+ *    Functions that return host values synchronise that stream.
+ *  - Host arrays use the reference's serde layouts:
+ *      links  : double[V*D][3 cols][3 rows][2]  column-major 3x3 complex (nalgebra),
+ *               link index = site*D + mu  (src/lattice.rs:925-929)
+ *      efield : double[V][D][8]           su(3) coefficients e^a of E = e^a T^a
+ *               (src/field.rs:1025-1027)
+ *      site   : sum_i x_i L^i, x_0 fastest (src/lattice.rs:909-916)
+ *  - D must be 2, 3 or 4; any other D returns LQ_ERR_UNSUPPORTED_DIM.
+ */
+#ifndef LQGPU_H
+#define LQGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+enum lq_status {
+    LQ_OK = 0,
+    /* LatticeInitializationError (src/error.rs:219-241) */
+    LQ_ERR_NON_POSITIVE_SIZE = 1,
+    LQ_ERR_DIM_TOO_SMALL = 2,
+    LQ_ERR_ZERO_DIMENSION = 3,
+    LQ_ERR_UNSUPPORTED_DIM = 4,
+    /* StateInitializationError (src/error.rs:124-171) */
+    LQ_ERR_INVALID_NORMAL = 5,      /* InvalidParameterNormalDistribution: 0.5/beta not a valid std dev */
+    LQ_ERR_INCOMPATIBLE_SIZE = 6,   /* IncompatibleSize */
+    LQ_ERR_GAUSS_PROJECTION = 7,    /* GaussProjectionError (NaN residual, src/field.rs:1282-1284) */
+    /* MultiIntegrationError (src/error.rs:93-118) */
+    LQ_ERR_ZERO_INTEGRATION = 8,    /* ZeroIntegration */
+    /* library errors without a reference counterpart */
+    LQ_ERR_INVALID_ARGUMENT = 9,
+    LQ_ERR_NOT_CONVERGED = 10,      /* Gauss projection reached max_steps (the reference loops forever) */
+    LQ_ERR_WRONG_STATE_KIND = 11,   /* leap-frog call on a synchronous state or vice versa */
+    LQ_ERR_NO_PENDING = 12,         /* lq_hmc_decide without a proposal */
+    LQ_ERR_CUDA = 20,               /* a CUDA runtime call failed (lq_last_error_string) */
+    LQ_ERR_OUT_OF_MEMORY = 21,
+    LQ_ERR_NO_DEVICE = 22
+};
+
+/* arithmetic of the state */
+enum lq_precision {
+    LQ_PRECISION_F64 = 0,   /* FP64 throughout: parity form */
+    LQ_PRECISION_MIXED = 1  /* FP32 links/E/force, FP64 reductions and reprojection */
+};
+
+/* SymplecticIntegrator methods (src/integrator/mod.rs:93-208) */
+enum lq_integration_mode {
+    LQ_SYNC_SYNC = 0,   /* integrate_sync_sync:  U += dt dU(E,U);  E += dt F(U)       (both from the old state) */
+    LQ_SYNC_LEAP = 1,   /* integrate_sync_leap:  E += dt/2 F(U)                       (state becomes leap-frog) */
+    LQ_LEAP_LEAP = 2,   /* integrate_leap_leap:  U += dt dU(E,U);  E += dt F(U')      */
+    LQ_LEAP_SYNC = 3,   /* integrate_leap_sync:  U += dt dU(E,U);  E += dt/2 F(U')    (state becomes synchronous) */
+    LQ_SYMPLECTIC = 4   /* integrate_symplectic: E += dt/2 F(U); U += dt dU(E,U); E += dt/2 F(U') */
+};
+
+typedef struct lq_state lq_state;
+
+/* ---------------------------------------------------------------- lifetime */
+
+/* LatticeCyclic::new (src/lattice.rs:190-201) + LatticeStateDefault::new_cold
+ * (src/simulation/state.rs:670-678) + LatticeStateEFSyncDefault::new_e_cold
+ * (src/simulation/state.rs:1111-1120): a state of V = L^dim sites with U = 1, E = 0, t = 0.
+ * size: the lattice spacing parameter (forces scale as 1/size); beta: coupling.
+ * Validation order and errors follow LatticeCyclic::new, then LQ_ERR_UNSUPPORTED_DIM. */
+int lq_state_create(int dim, int L, double size, double beta, int precision, lq_state **out);
+int lq_state_destroy(lq_state *s);
+/* Clone for State: Clone (src/simulation/monte_carlo/hybrid_monte_carlo.rs:318); same stream. */
+int lq_state_clone(const lq_state *s, lq_state **out);
+/* Attach a cudaStream_t (passed as void*); NULL selects the legacy default stream. */
+int lq_state_set_stream(lq_state *s, void *cuda_stream);
+/* Getters: LatticeCyclic::dim/size, LatticeState::beta, LatticeStateWithEField::t,
+ * number_of_points (src/lattice.rs:208-233). is_leap = 1 between sync_leap and leap_sync. */
+int lq_state_info(const lq_state *s, int *dim, int *L, double *size, double *beta, int *precision,
+                  long long *n_sites, long long *t, int *is_leap);
+int lq_state_set_beta(lq_state *s, double beta);
+/* Device bytes held by the state (links buffers, E, Gauss buffer, staging). */
+int lq_state_device_bytes(const lq_state *s, size_t *bytes);
+
+/* ---------------------------------------------------------------- fields */
+
+/* LatticeState::set_link_matrix / link_matrix (src/simulation/state.rs:73-81, :808-815).
+ * n_doubles must be V*D*18, else LQ_ERR_INCOMPATIBLE_SIZE (the reference panics). */
+int lq_links_upload(lq_state *s, const double *links, size_t n_doubles);
+int lq_links_download(lq_state *s, double *links, size_t n_doubles);
+/* LinkMatrix::new_cold (src/field.rs:703-707) */
+int lq_links_set_cold(lq_state *s);
+/* LinkMatrix::new_determinist with su3::random_su3 (src/field.rs:646-659, src/su3.rs:322-355),
+ * drawn on the device from a Philox4x32-10 stream keyed by seed (not the Rust RNG stream). */
+int lq_links_random(lq_state *s, uint64_t seed);
+
+/* LatticeStateWithEField::set_e_field / e_field (src/simulation/state.rs:1387-1399).
+ * n_doubles must be V*D*8. */
+int lq_efield_upload(lq_state *s, const double *efield, size_t n_doubles);
+int lq_efield_download(lq_state *s, double *efield, size_t n_doubles);
+/* EField::new_cold (src/field.rs:1126-1131) */
+int lq_efield_set_cold(lq_state *s);
+/* EField::new_determinist with Normal(0, std_dev) (src/field.rs:1086-1099): every coefficient
+ * drawn on the device (Philox4x32-10 + Box-Muller) from (seed, counter). */
+int lq_efield_random_normal(lq_state *s, uint64_t seed, uint64_t counter, double std_dev);
+
+/* ---------------------------------------------------------------- observables */
+
+/* LatticeState::hamiltonian_links (src/simulation/state.rs:821-849): beta sum_x sum_{mu<nu} (1 - Re Tr P/3) */
+int lq_hamiltonian_links(lq_state *s, double *out);
+/* LatticeStateWithEField::hamiltonian_efield (src/simulation/state.rs:1370-1385): beta sum e^2/2 */
+int lq_hamiltonian_efield(lq_state *s, double *out);
+/* LatticeStateWithEField::hamiltonian_total (src/simulation/state.rs:229-231) */
+int lq_hamiltonian_total(lq_state *s, double *out);
+/* LatticeState::average_trace_plaquette (src/field.rs:775-804): sum Tr P / (V D(D-1)/2) */
+int lq_average_trace_plaquette(lq_state *s, double *re, double *im);
+/* EField::gauss_sum_div (src/field.rs:1199-1220): sum_x |Tr((sum_a T^a) G(x))| */
+int lq_gauss_sum_div(lq_state *s, double *out);
+/* EField::gauss at every site (src/field.rs:1174-1195), as 8 coefficients g^a = 2 Re Tr(T^a G(x)),
+ * out: double[V][8]. */
+int lq_gauss_download(lq_state *s, double *out, size_t n_doubles);
+
+/* ---------------------------------------------------------------- updates */
+
+/* EField::project_to_gauss (src/field.rs:1265-1294): one projection step, then blocks of four
+ * until gauss_sum_div <= eps * V * 320 (eps of the state's storage type).  max_steps > 0 caps
+ * the steps (LQ_ERR_NOT_CONVERGED); a NaN residual gives LQ_ERR_GAUSS_PROJECTION. */
+int lq_project_gauss(lq_state *s, int max_steps, int *steps_done);
+/* LatticeStateDefault::normalize_link_matrices (src/simulation/state.rs:754-756):
+ * su3::orthonormalize_matrix on every link (src/su3.rs:290-309), computed in FP64. */
+int lq_normalize_link_matrices(lq_state *s);
+
+/* SymplecticIntegrator for SymplecticEulerRayon (src/integrator/symplectic_euler_rayon.rs:120-252),
+ * repeated n times as simulate_*_n does (src/simulation/state.rs:399-491, :603-647).
+ * n == 0 gives LQ_ERR_ZERO_INTEGRATION.  SYNC_LEAP requires a synchronous state and leaves a
+ * leap-frog state; LEAP_LEAP requires leap-frog; LEAP_SYNC requires leap-frog and leaves a
+ * synchronous state; SYNC_SYNC / SYMPLECTIC require a synchronous state (else
+ * LQ_ERR_WRONG_STATE_KIND).  t advances as in the reference (sync_leap does not advance it). */
+int lq_integrate(lq_state *s, int mode, double dt, int n);
+/* simulate_using_leapfrog_n (src/simulation/state.rs:318-357) */
+int lq_leapfrog_n(lq_state *s, double dt, int n);
+
+/* ---------------------------------------------------------------- HMC
+ * HybridMonteCarloDiagnostic::next_element (src/simulation/monte_carlo/hybrid_monte_carlo.rs:465-471,
+ * :573-613), split as the reference splits it:
+ *   refresh     : new_random_e_state (src/simulation/state.rs:1093-1108) -- draw E ~ N(0, 0.5/beta)
+ *                 then project_to_gauss; lq_hmc_refresh draws on the device, lq_hmc_refresh_upload
+ *                 takes the drawn field from the host (test mode).
+ *   propose     : simulate_symplectic_n_auto(dt, n) + probability_of_replacement
+ *                 prob = clamp(exp(H_old - H_new), 0, 1); the start state is kept.
+ *   decide      : Bernoulli(prob) -- accept = 1 keeps the proposal, 0 restores the start state
+ *                 (LatticeStateDefault only: the E-field is dropped by state_owned).
+ *   trajectory  : all four with accept = (prob >= 1 || uniform < prob), the rand 0.8 Bernoulli rule. */
+int lq_hmc_refresh(lq_state *s, uint64_t seed, uint64_t counter, int max_gauss_steps, int *gauss_steps);
+int lq_hmc_refresh_upload(lq_state *s, const double *efield_raw, size_t n_doubles, int max_gauss_steps,
+                          int *gauss_steps);
+int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_old, double *h_new);
+int lq_hmc_decide(lq_state *s, int accept);
+int lq_hmc_trajectory(lq_state *s, double dt, int n_steps, uint64_t seed, uint64_t counter, double uniform,
+                      int max_gauss_steps, int *accepted, double *prob, double *delta_h, int *gauss_steps);
+
+/* ---------------------------------------------------------------- profiling
+ * Per-kernel-class launch counters timed with CUDA events on the state's stream (no
+ * reference counterpart: the reference has no tracing).  While enabled, every launch of
+ * the state is bracketed by an event pair; totals accumulate at each synchronisation. */
+enum lq_kernel_class {
+    LQ_KERNEL_MD = 0,         /* fused force/kick/drift (k_md) */
+    LQ_KERNEL_GAUSS = 1,      /* Gauss law G(x) + residual partials (k_gauss) */
+    LQ_KERNEL_GAUSS_STEP = 2, /* projection step (k_gauss_step) */
+    LQ_KERNEL_PLAQUETTE = 3,  /* plaquette / hamiltonian_links partials (k_plaquette) */
+    LQ_KERNEL_REDUCE = 4,     /* sum of squares and final reductions */
+    LQ_KERNEL_OTHER = 5,      /* layout conversion, initialisation, reprojection */
+    LQ_KERNEL_CLASSES = 6
+};
+int lq_profile_enable(lq_state *s, int on);
+/* launches and total milliseconds of one class since the last reset; also resets when reset != 0 */
+int lq_profile_read(lq_state *s, int kernel_class, long long *launches, double *total_ms, int reset);
+
+/* ---------------------------------------------------------------- diagnostics */
+const char *lq_status_string(int status);
+/* Text of the last error on this host thread (CUDA error name and call site). */
+const char *lq_last_error_string(void);
+/* Library version (major*10000 + minor*100 + patch). */
+int lq_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LQGPU_H */

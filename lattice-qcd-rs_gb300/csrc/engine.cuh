@@ -1,0 +1,130 @@
+// engine.cuh -- launch wrappers of the device kernels for one (D, T) instantiation.
+#pragma once
+#include <math.h>
+
+#include "kernels.cuh"
+#include "state.hpp"
+
+namespace lq {
+
+template <int D, typename T> struct Engine {
+    static Geo<D> geo(const State &s) {
+        Geo<D> g;
+        g.V = s.V;
+        g.L = (uint32_t)s.L;
+        uint32_t st = 1;
+        for (int i = 0; i < 4; ++i) {
+            g.stride[i] = st;
+            if (i < D) st *= (uint32_t)s.L;
+        }
+        return g;
+    }
+    static dim3 link_grid(const State &s, int threads) { return dim3((s.V + threads - 1) / threads, D, 1); }
+
+    static cudaError_t links_from_aos(State &s, const double *d_aos, void *dst) {
+        k_links_from_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (V2<T> *)dst, s.V);
+        return cudaGetLastError();
+    }
+    static cudaError_t links_to_aos(State &s, const void *src, double *d_aos) {
+        k_links_to_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)src, d_aos, s.V);
+        return cudaGetLastError();
+    }
+    static cudaError_t links_cold(State &s, void *dst) {
+        k_links_identity<T><<<1024, 256, 0, s.stream>>>((V2<T> *)dst, (size_t)s.V, D);
+        return cudaGetLastError();
+    }
+    static cudaError_t links_random(State &s, void *dst, uint64_t seed) {
+        const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+        k_links_random<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, s.V, key);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_normalize<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, geo(s));
+        return cudaGetLastError();
+    }
+    static cudaError_t efield_from_aos(State &s, const double *d_aos) {
+        k_efield_from_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V);
+        return cudaGetLastError();
+    }
+    static cudaError_t efield_to_aos(State &s, double *d_aos) {
+        k_efield_to_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)s.E, d_aos, s.V);
+        return cudaGetLastError();
+    }
+    static cudaError_t efield_normal(State &s, uint64_t seed, uint64_t counter, double sd) {
+        const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+        k_efield_normal<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((T *)s.E, s.V, key, (uint32_t)counter,
+                                                                         (uint32_t)(counter >> 32), (T)sd);
+        return cudaGetLastError();
+    }
+    static cudaError_t md(State &s, const void *Uin, void *Uout, int mode, double h1, double h2, double dt) {
+        // kick coefficient h * c_e / size with c_e = -sqrt(2 / C_A), C_A = 3
+        const double ce = -sqrt(2.0 / 3.0) / s.size;
+        // drift coefficient dt * sqrt(2 C_A) / size
+        const double cu = sqrt(2.0 * 3.0) / s.size * dt;
+        const T k1 = (T)(h1 * ce), k2 = (T)(h2 * ce), drift = (T)cu;
+        const Geo<D> g = geo(s);
+        const dim3 grid = link_grid(s, 128);
+        const V2<T> *in = (const V2<T> *)Uin;
+        V2<T> *out = (V2<T> *)Uout;
+        T *E = (T *)s.E;
+        switch (mode) {
+        case MD_KICK: k_md<D, T, MD_KICK><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift); break;
+        case MD_DRIFT: k_md<D, T, MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift); break;
+        case MD_KICK | MD_DRIFT:
+            k_md<D, T, MD_KICK | MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift);
+            break;
+        case MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E:
+            k_md<D, T, MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift);
+            break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
+    static cudaError_t gauss(State &s, const void *U, uint32_t *n_partials) {
+        const uint32_t blocks = (s.V + 255) / 256;
+        k_gauss<D, T><<<blocks, 256, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.G, geo(s), s.partial);
+        *n_partials = blocks;
+        return cudaGetLastError();
+    }
+    static cudaError_t gauss_step(State &s, const void *U) {
+        k_gauss_step<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)U, (T *)s.E, (const T *)s.G,
+                                                                       geo(s));
+        return cudaGetLastError();
+    }
+    static cudaError_t gauss_to_aos(State &s, double *d_out) {
+        k_gauss_to_aos<T><<<(s.V + 255) / 256, 256, 0, s.stream>>>((const T *)s.G, d_out, s.V);
+        return cudaGetLastError();
+    }
+    static cudaError_t plaquette(State &s, const void *U, uint32_t *n_partials) {
+        const uint32_t blocks = (s.V + 127) / 128;
+        k_plaquette<D, T><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, geo(s), s.partial);
+        *n_partials = blocks;
+        return cudaGetLastError();
+    }
+    static cudaError_t efield_sumsq(State &s, uint32_t *n_partials) {
+        const uint32_t blocks = 1024;
+        k_sum_squares<T><<<blocks, 256, 0, s.stream>>>((const T *)s.E, s.efield_elems(), s.partial);
+        *n_partials = blocks;
+        return cudaGetLastError();
+    }
+    static cudaError_t normalize(State &s, void *U) {
+        k_normalize<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)U, geo(s));
+        return cudaGetLastError();
+    }
+    static cudaError_t finalize(State &s, int nv, uint32_t n, int offset) {
+        switch (nv) {
+        case 1: k_finalize<1><<<1, 1024, 0, s.stream>>>(s.partial, n, s.d_out + offset); break;
+        case 3: k_finalize<3><<<1, 1024, 0, s.stream>>>(s.partial, n, s.d_out + offset); break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
+
+    static const Ops *table() {
+        static const Ops ops = {links_from_aos, links_to_aos, links_cold,   links_random, efield_from_aos,
+                                efield_to_aos,  efield_normal, md,          gauss,        gauss_step,
+                                gauss_to_aos,   plaquette,     efield_sumsq, normalize,    finalize};
+        return &ops;
+    }
+};
+
+} // namespace lq

@@ -1,0 +1,599 @@
+// kernels.cuh -- device kernels of the HMC molecular-dynamics path, templated on the
+// lattice dimension D (2, 3, 4) and the storage/compute type T (double or float).
+//
+// Device layout (structure of arrays, one plane per matrix/vector component):
+//   links  U : vec2<T>[D][9][V]   U[(mu*9 + k)*V + site], k = row*3 + col
+//   efield E : T[D][8][V]          E[(mu*8 + a)*V + site]
+//   gauss  G : T[8][V]             g^a(x) = 2 Re Tr(T^a G(x))
+// Sites are linearised x_0 fastest as in the reference (src/lattice.rs:909-916), so the
+// +-mu neighbour of a site is +-L^mu with periodic wrap, and consecutive threads touch
+// consecutive addresses of every plane (coalesced 128-bit/64-bit accesses).
+#pragma once
+#include "su3.cuh"
+
+namespace lq {
+
+template <int D> struct Geo {
+    uint32_t V;         // number of sites L^D
+    uint32_t L;         // points per direction
+    uint32_t stride[4]; // L^mu
+};
+
+template <int D> __device__ __forceinline__ void site_coords(const Geo<D> &g, uint32_t site, uint32_t *c) {
+#pragma unroll
+    for (int i = 0; i < D; ++i) c[i] = (site / g.stride[i]) % g.L;
+}
+// neighbour of `site` (whose coordinate along mu is cmu) in +mu / -mu, periodic
+template <int D>
+__device__ __forceinline__ uint32_t fwd(const Geo<D> &g, uint32_t site, uint32_t cmu, int mu) {
+    return (cmu == g.L - 1) ? site - (g.L - 1) * g.stride[mu] : site + g.stride[mu];
+}
+template <int D>
+__device__ __forceinline__ uint32_t bwd(const Geo<D> &g, uint32_t site, uint32_t cmu, int mu) {
+    return (cmu == 0) ? site + (g.L - 1) * g.stride[mu] : site - g.stride[mu];
+}
+
+template <typename T> using V2 = typename vec2_t<T>::type;
+
+// ------------------------------------------------------------------ block reductions
+// Fixed-shape warp-shuffle + shared-memory tree: deterministic for a given launch shape.
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *__restrict__ out, uint32_t slot,
+                                                   uint32_t nslots) {
+    __shared__ double red[32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) red[warp][i] = v[i];
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double x = (lane < nw) ? red[lane][i] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) out[(size_t)i * nslots + slot] = x;
+        }
+    }
+}
+
+// Sum NV rows of `n` partials each, in a fixed order, into out[0..NV).  One block of 1024.
+template <int NV>
+__global__ void __launch_bounds__(1024) k_finalize(const double *__restrict__ partial, uint32_t n, double *out) {
+    double v[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double s = 0.0;
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) s += partial[(size_t)i * n + k];
+        v[i] = s;
+    }
+    double tmp[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) tmp[i] = v[i];
+    block_reduce_store<NV>(tmp, out, 0, 1);
+}
+
+// ------------------------------------------------------------------ gauge force
+// Staple sum of link (x, mu) in the reference's order of directions [+0,-0,+1,-1,...]
+// skipping +-mu (procedural_macro/src/lib.rs:53-83, src/simulation/state.rs:1428-1437):
+//   +nu : U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag            = S_mu,nu(x)^dag
+//   -nu : U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)      = S_mu,-nu(x)^dag
+template <int D, typename T>
+__device__ __forceinline__ void staple_sum(const V2<T> *__restrict__ U, const Geo<D> &g, uint32_t site,
+                                           const uint32_t *c, int mu, mat3<T> &sig) {
+    const size_t V = g.V;
+    const uint32_t xpmu = fwd(g, site, c[mu], mu);
+    mat_zero(sig);
+#pragma unroll
+    for (int nu = 0; nu < D; ++nu) {
+        if (nu == mu) continue;
+        {
+            mat3<T> a, b, t;
+            load_link<T>(U, (size_t)(nu * 9) * V, V, xpmu, a);
+            load_link<T>(U, (size_t)(mu * 9) * V, V, fwd(g, site, c[nu], nu), b);
+            mul_na(a, b, t);
+            load_link<T>(U, (size_t)(nu * 9) * V, V, site, a);
+            mul_na_acc(t, a, sig);
+        }
+        {
+            mat3<T> a, b, w;
+            const uint32_t xmnu = bwd(g, site, c[nu], nu);
+            load_link<T>(U, (size_t)(mu * 9) * V, V, xmnu, a);
+            load_link<T>(U, (size_t)(nu * 9) * V, V, bwd(g, xpmu, c[nu], nu), b);
+            mul_nn(a, b, w);
+            load_link<T>(U, (size_t)(nu * 9) * V, V, xmnu, a);
+            mul_an_acc(w, a, sig);
+        }
+    }
+}
+
+enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4 };
+
+// One thread per link (site = x index, mu = blockIdx.y).
+//  KICK : F^a = Im Tr(T^a U_mu(x) Sigma(x)) (derivative_e, src/simulation/state.rs:1420-1448);
+//         e += k1 * F (when k1 != 0), then e += k2 * F, with k = h * c_e / size,
+//         c_e = -sqrt(2/C_A).  Two separate adds keep the reference's rounding of a step end
+//         followed by the next step's start (src/integrator/symplectic_euler_rayon.rs:222-252).
+//  DRIFT: U' = U + drift * i (E U), drift = dt sqrt(2 C_A) / size
+//         (derivative_u + integrate_link, src/simulation/state.rs:1407-1417,
+//          src/integrator/mod.rs:216-233), with E after the kick or, with DRIFT_OLD_E,
+//         before it (integrate_sync_sync integrates both fields from the old state).
+template <int D, typename T, int MODE>
+__global__ void __launch_bounds__(128) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout,
+                                            T *__restrict__ E, Geo<D> g, T k1, T k2, T drift) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= g.V) return;
+    const size_t V = g.V;
+    uint32_t c[D];
+    site_coords(g, site, c);
+    T e[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) e[a] = E[(size_t)(mu * 8 + a) * V + site];
+    mat3<T> u;
+    load_link<T>(Uin, (size_t)(mu * 9) * V, V, site, u);
+    T e_old[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) e_old[a] = e[a];
+    if (MODE & MD_KICK) {
+        mat3<T> sig, m;
+        staple_sum<D, T>(Uin, g, site, c, mu, sig);
+        mul_nn(u, sig, m);
+        T f[8];
+        im_tr_generators(m, f);
+        if (k1 != T(0)) {
+#pragma unroll
+            for (int a = 0; a < 8; ++a) e[a] = fma(k1, f[a], e[a]);
+        }
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            e[a] = fma(k2, f[a], e[a]);
+            E[(size_t)(mu * 8 + a) * V + site] = e[a];
+        }
+    }
+    if (MODE & MD_DRIFT) {
+        mat3<T> em, w;
+        adjoint_to_matrix<T>((MODE & MD_DRIFT_OLD_E) ? e_old : e, em);
+        mul_nn(em, u, w);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            u.e[k].re = fma(-drift, w.e[k].im, u.e[k].re);
+            u.e[k].im = fma(drift, w.e[k].re, u.e[k].im);
+        }
+        store_link<T>(Uout, (size_t)(mu * 9) * V, V, site, u);
+    }
+}
+
+// ------------------------------------------------------------------ Gauss law
+// G(x) = sum_mu [E_mu(x) - U_mu(x-mu)^dag E_mu(x-mu) U_mu(x-mu)]  (EField::gauss,
+// src/field.rs:1174-1195), stored as 8 coefficients; the per-site residual
+// |Tr((sum_a T^a) G(x))| = |sum_a g^a| / 2 (gauss_sum_div, src/field.rs:1199-1220) is
+// reduced into one partial per block.
+template <int D, typename T>
+__global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, const T *__restrict__ E,
+                                               T *__restrict__ G, Geo<D> g, double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double r[1] = {0.0};
+    if (site < g.V) {
+        const size_t V = g.V;
+        uint32_t c[D];
+        site_coords(g, site, c);
+        T gs[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) gs[a] = T(0);
+#pragma unroll
+        for (int mu = 0; mu < D; ++mu) {
+            const uint32_t xm = bwd(g, site, c[mu], mu);
+            T em_c[8];
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                gs[a] += E[(size_t)(mu * 8 + a) * V + site];
+                em_c[a] = E[(size_t)(mu * 8 + a) * V + xm];
+            }
+            mat3<T> u, em, t, w;
+            load_link<T>(U, (size_t)(mu * 9) * V, V, xm, u);
+            adjoint_to_matrix<T>(em_c, em);
+            mul_nn(em, u, t);
+            mul_an(u, t, w);
+            T wc[8];
+            two_re_tr_generators(w, wc);
+#pragma unroll
+            for (int a = 0; a < 8; ++a) gs[a] -= wc[a];
+        }
+        double s = 0.0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            G[(size_t)a * V + site] = gs[a];
+            s += (double)gs[a];
+        }
+        r[0] = fabs(s) * 0.5;
+    }
+    block_reduce_store<1>(r, partial, blockIdx.x, gridDim.x);
+}
+
+// One projection step on link (x, mu) (EField::project_to_gauss_step, src/field.rs:1301-1337):
+//   e'^a = 2 Re Tr(T^a [(u G(x) u^dag G(x+mu) - G(x)) K + T^a e^a]),  K = 0.12
+//        = e^a + K (2 Re Tr(T^a u G(x) u^dag G(x+mu)) - g^a(x))
+// E is updated in place: each thread reads and writes only its own link.
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U, T *__restrict__ E,
+                                                    const T *__restrict__ G, Geo<D> g) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= g.V) return;
+    const size_t V = g.V;
+    uint32_t c[D];
+    site_coords(g, site, c);
+    const uint32_t xp = fwd(g, site, c[mu], mu);
+    T gx[8], gp[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        gx[a] = G[(size_t)a * V + site];
+        gp[a] = G[(size_t)a * V + xp];
+    }
+    mat3<T> u, gm, gpm, t1, t2, x;
+    load_link<T>(U, (size_t)(mu * 9) * V, V, site, u);
+    adjoint_to_matrix<T>(gx, gm);
+    adjoint_to_matrix<T>(gp, gpm);
+    mul_nn(u, gm, t1);
+    mul_na(t1, u, t2);
+    mul_nn(t2, gpm, x);
+    T xc[8];
+    two_re_tr_generators(x, xc);
+    const T K = T(0.12);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        const size_t idx = (size_t)(mu * 8 + a) * V + site;
+        E[idx] = fma(K, xc[a] - gx[a], E[idx]);
+    }
+}
+
+// ------------------------------------------------------------------ plaquettes
+// Per site, for mu < nu: P = U_mu(x) U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag
+// (pij, src/field.rs:761-771), Tr P = Tr(A B^dag) with A = U_mu(x) U_nu(x+mu),
+// B = U_nu(x) U_mu(x+nu).  Partials: [0] sum (1 - Re Tr P / 3) (hamiltonian_links,
+// src/simulation/state.rs:821-849), [1] sum Re Tr P, [2] sum Im Tr P
+// (average_trace_plaquette, src/field.rs:775-804); the per-plaquette traces are in T and
+// every sum is in double.
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, Geo<D> g,
+                                                   double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if (site < g.V) {
+        const size_t V = g.V;
+        uint32_t c[D];
+        site_coords(g, site, c);
+#pragma unroll
+        for (int mu = 0; mu < D; ++mu) {
+            const uint32_t xpmu = fwd(g, site, c[mu], mu);
+#pragma unroll
+            for (int nu = mu + 1; nu < D; ++nu) {
+                mat3<T> p, q, A, B;
+                load_link<T>(U, (size_t)(mu * 9) * V, V, site, p);
+                load_link<T>(U, (size_t)(nu * 9) * V, V, xpmu, q);
+                mul_nn(p, q, A);
+                load_link<T>(U, (size_t)(nu * 9) * V, V, site, p);
+                load_link<T>(U, (size_t)(mu * 9) * V, V, fwd(g, site, c[nu], nu), q);
+                mul_nn(p, q, B);
+                T re = T(0), im = T(0);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    re = fma(A.e[k].re, B.e[k].re, re);
+                    re = fma(A.e[k].im, B.e[k].im, re);
+                    im = fma(A.e[k].im, B.e[k].re, im);
+                    im = fma(-A.e[k].re, B.e[k].im, im);
+                }
+                v[0] += 1.0 - (double)re / 3.0;
+                v[1] += (double)re;
+                v[2] += (double)im;
+            }
+        }
+    }
+    block_reduce_store<3>(v, partial, blockIdx.x, gridDim.x);
+}
+
+// sum of squares of n values (hamiltonian_efield before the beta/2 factor), in double
+template <typename T>
+__global__ void __launch_bounds__(256) k_sum_squares(const T *__restrict__ x, size_t n, double *__restrict__ partial) {
+    double v[1] = {0.0};
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double y = (double)x[i];
+        v[0] = fma(y, y, v[0]);
+    }
+    block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
+}
+
+// ------------------------------------------------------------------ reprojection
+// orthonormalize_matrix (src/su3.rs:290-309), computed in double for either storage type:
+// v1 = col0 / |col0|, v2 = col1 - v1 (v1^* . col1), normalised, col2 = conj(v1) x conj(v2);
+// a vector whose norm is <= f64::EPSILON is kept unnormalised (try_normalize).
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D> g) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= g.V) return;
+    const size_t V = g.V;
+    const size_t p0 = (size_t)(mu * 9) * V;
+    double r1[3], i1[3], r2[3], i2[3];
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+        const V2<T> a = U[p0 + (size_t)(row * 3 + 0) * V + site];
+        const V2<T> b = U[p0 + (size_t)(row * 3 + 1) * V + site];
+        r1[row] = a.x;
+        i1[row] = a.y;
+        r2[row] = b.x;
+        i2[row] = b.y;
+    }
+    const double eps = 2.220446049250313e-16;
+    double n1 = sqrt(r1[0] * r1[0] + i1[0] * i1[0] + r1[1] * r1[1] + i1[1] * i1[1] + r1[2] * r1[2] + i1[2] * i1[2]);
+    if (n1 > eps) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            r1[k] /= n1;
+            i1[k] /= n1;
+        }
+    }
+    // proj = sum_k conj(v1_k) v2_k
+    double pr = 0.0, pi = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        pr += r1[k] * r2[k] + i1[k] * i2[k];
+        pi += r1[k] * i2[k] - i1[k] * r2[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double tr = r1[k] * pr - i1[k] * pi;
+        const double ti = r1[k] * pi + i1[k] * pr;
+        r2[k] -= tr;
+        i2[k] -= ti;
+    }
+    const double n2 =
+        sqrt(r2[0] * r2[0] + i2[0] * i2[0] + r2[1] * r2[1] + i2[1] * i2[1] + r2[2] * r2[2] + i2[2] * i2[2]);
+    if (n2 > eps) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            r2[k] /= n2;
+            i2[k] /= n2;
+        }
+    }
+    // col2 = conj(v1) x conj(v2): (a x b)_k with a = conj(v1), b = conj(v2)
+    double r3[3], i3[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+        // a_k1 b_k2 - a_k2 b_k1 with a = (r1, -i1), b = (r2, -i2)
+        const double xr = r1[k1] * r2[k2] - i1[k1] * i2[k2];
+        const double xi = -(r1[k1] * i2[k2] + i1[k1] * r2[k2]);
+        const double yr = r1[k2] * r2[k1] - i1[k2] * i2[k1];
+        const double yi = -(r1[k2] * i2[k1] + i1[k2] * r2[k1]);
+        r3[k] = xr - yr;
+        i3[k] = xi - yi;
+    }
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+        V2<T> a, b, cc;
+        a.x = (T)r1[row];
+        a.y = (T)i1[row];
+        b.x = (T)r2[row];
+        b.y = (T)i2[row];
+        cc.x = (T)r3[row];
+        cc.y = (T)i3[row];
+        U[p0 + (size_t)(row * 3 + 0) * V + site] = a;
+        U[p0 + (size_t)(row * 3 + 1) * V + site] = b;
+        U[p0 + (size_t)(row * 3 + 2) * V + site] = cc;
+    }
+}
+
+// ------------------------------------------------------------------ layout conversion
+// host serde layout (double AoS, column-major complex 3x3 per link) <-> device SoA planes
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_links_from_aos(const double *__restrict__ aos, V2<T> *__restrict__ U,
+                                                        uint32_t V) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    const double *src = aos + ((size_t)site * D + mu) * 18;
+#pragma unroll
+    for (int col = 0; col < 3; ++col)
+#pragma unroll
+        for (int row = 0; row < 3; ++row) {
+            V2<T> v;
+            v.x = (T)src[(col * 3 + row) * 2];
+            v.y = (T)src[(col * 3 + row) * 2 + 1];
+            U[(size_t)(mu * 9 + row * 3 + col) * V + site] = v;
+        }
+}
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ U, double *__restrict__ aos,
+                                                      uint32_t V) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    double *dst = aos + ((size_t)site * D + mu) * 18;
+#pragma unroll
+    for (int col = 0; col < 3; ++col)
+#pragma unroll
+        for (int row = 0; row < 3; ++row) {
+            const V2<T> v = U[(size_t)(mu * 9 + row * 3 + col) * V + site];
+            dst[(col * 3 + row) * 2] = (double)v.x;
+            dst[(col * 3 + row) * 2 + 1] = (double)v.y;
+        }
+}
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restrict__ aos, T *__restrict__ E,
+                                                         uint32_t V) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    const double *src = aos + ((size_t)site * D + mu) * 8;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) E[(size_t)(mu * 8 + a) * V + site] = (T)src[a];
+}
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, double *__restrict__ aos,
+                                                       uint32_t V) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    double *dst = aos + ((size_t)site * D + mu) * 8;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) dst[a] = (double)E[(size_t)(mu * 8 + a) * V + site];
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_gauss_to_aos(const T *__restrict__ G, double *__restrict__ out, uint32_t V) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    if (site >= V) return;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) out[(size_t)site * 8 + a] = (double)G[(size_t)a * V + site];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_links_identity(V2<T> *__restrict__ U, size_t V, int D) {
+    const size_t n = V * 9 * D;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)((i / V) % 9);
+        V2<T> v;
+        v.x = (k == 0 || k == 4 || k == 8) ? T(1) : T(0);
+        v.y = T(0);
+        U[i] = v;
+    }
+}
+
+// ------------------------------------------------------------------ Philox4x32-10
+// Counter-based generator of Salmon, Moraes, Dror & Shaw (SC'11): 10 rounds of the
+// 4x32 S-box with multipliers 0xD2511F53 / 0xCD9E8D57 and Weyl key increments
+// 0x9E3779B9 / 0xBB67AE85.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k.x += 0x9E3779B9u;
+            k.y += 0xBB67AE85u;
+        }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+// [0,1) with 53 random bits
+__device__ __forceinline__ double u01_53(uint32_t hi, uint32_t lo) {
+    const uint64_t v = (((uint64_t)hi << 32) | lo) >> 11;
+    return (double)v * 0x1.0p-53;
+}
+// [0,1) with 24 random bits
+__device__ __forceinline__ float u01_24(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }
+
+// Box-Muller pair from two uniforms in [0,1)
+__device__ __forceinline__ void box_muller(double u1, double u2, double &z0, double &z1) {
+    const double r = sqrt(-2.0 * log(1.0 - u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+__device__ __forceinline__ void box_muller(float u1, float u2, float &z0, float &z1) {
+    const float r = sqrtf(-2.0f * logf(1.0f - u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+
+// E^a(x, mu) ~ Normal(0, sd), independent per (link, a); counter = (link, ctr_lo, ctr_hi, call)
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32_t V, uint2 key, uint32_t ctr_lo,
+                                                       uint32_t ctr_hi, T sd) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    const uint32_t link = site * D + mu;
+    T z[8];
+    if (sizeof(T) == 8) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint4 r = philox4x32_10(make_uint4(link, ctr_lo, ctr_hi, (uint32_t)j), key);
+            double a, b;
+            box_muller(u01_53(r.x, r.y), u01_53(r.z, r.w), a, b);
+            z[2 * j] = (T)a;
+            z[2 * j + 1] = (T)b;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const uint4 r = philox4x32_10(make_uint4(link, ctr_lo, ctr_hi, (uint32_t)j), key);
+            float a, b, c2, d2;
+            box_muller(u01_24(r.x), u01_24(r.y), a, b);
+            box_muller(u01_24(r.z), u01_24(r.w), c2, d2);
+            z[4 * j] = (T)a;
+            z[4 * j + 1] = (T)b;
+            z[4 * j + 2] = (T)c2;
+            z[4 * j + 3] = (T)d2;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 8; ++a) E[(size_t)(mu * 8 + a) * V + site] = z[a] * sd;
+}
+
+// random_su3 (src/su3.rs:322-355) per link: two complex 3-vectors with Uniform(-1,1)
+// entries, redrawn while |v1| <= eps or |v1 . v2| <= eps, then Gram-Schmidt and
+// col2 = conj(v1) x conj(v2); computed in double, stored as T.
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uint32_t V, uint2 key) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    const uint32_t link = site * D + mu;
+    const double eps = 2.220446049250313e-16;
+    double r1[3], i1[3], r2[3], i2[3];
+    uint32_t call = 0;
+    auto draw6 = [&](double *re, double *im) {
+        // 6 uniforms from 3 Philox blocks (53 bits each)
+        double u[6];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const uint4 r = philox4x32_10(make_uint4(link, call++, 0x53553300u, 0u), key);
+            u[2 * j] = u01_53(r.x, r.y);
+            u[2 * j + 1] = u01_53(r.z, r.w);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            re[k] = u[2 * k] * 2.0 - 1.0;
+            im[k] = u[2 * k + 1] * 2.0 - 1.0;
+        }
+    };
+    for (int tries = 0; tries < 64; ++tries) {
+        draw6(r1, i1);
+        const double n = r1[0] * r1[0] + i1[0] * i1[0] + r1[1] * r1[1] + i1[1] * i1[1] + r1[2] * r1[2] + i1[2] * i1[2];
+        if (sqrt(n) > eps) break;
+    }
+    for (int tries = 0; tries < 64; ++tries) {
+        draw6(r2, i2);
+        double dr = 0.0, di = 0.0; // non-conjugating dot
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            dr += r1[k] * r2[k] - i1[k] * i2[k];
+            di += r1[k] * i2[k] + i1[k] * r2[k];
+        }
+        if (hypot(dr, di) > eps) break;
+    }
+    const size_t p0 = (size_t)(mu * 9) * V;
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+        V2<T> a, b;
+        a.x = (T)r1[row];
+        a.y = (T)i1[row];
+        b.x = (T)r2[row];
+        b.y = (T)i2[row];
+        U[p0 + (size_t)(row * 3 + 0) * V + site] = a;
+        U[p0 + (size_t)(row * 3 + 1) * V + site] = b;
+    }
+}
+
+} // namespace lq

@@ -1,0 +1,771 @@
+// lq_api.cu -- the extern "C" entry points declared in include/lqgpu.h.
+//
+// Host orchestration of the device state: validation with the reference's error
+// taxonomy, buffer management, the integrator schedules and the HMC trajectory.  All
+// device work is enqueued on the state's stream; functions that hand a value back to the
+// host synchronise that stream once.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "kernels.cuh"
+#include "lqgpu.h"
+#include "state.hpp"
+
+using lq::State;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int cuda_fail(cudaError_t e, const char *what, int line) {
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s (%s) in %s at lq_api.cu:%d", cudaGetErrorName(e), cudaGetErrorString(e), what,
+             line);
+    g_last_error = buf;
+    (void)cudaGetLastError(); // clear a non-sticky error so the context stays usable
+    if (e == cudaErrorMemoryAllocation) return LQ_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return LQ_ERR_NO_DEVICE;
+    return LQ_ERR_CUDA;
+}
+
+#define LQ_CK(call)                                                                                                    \
+    do {                                                                                                               \
+        cudaError_t _e = (call);                                                                                       \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call, __LINE__);                                                  \
+    } while (0)
+
+#define LQ_LAUNCH(st, cls, call)                                                                                       \
+    do {                                                                                                               \
+        const int _slot = prof_begin(st);                                                                              \
+        cudaError_t _e = (call);                                                                                       \
+        prof_end(st, _slot, cls);                                                                                      \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call, __LINE__);                                                  \
+    } while (0)
+
+#define LQ_CHECK_STATE(s)                                                                                              \
+    do {                                                                                                               \
+        if (!(s)) return LQ_ERR_INVALID_ARGUMENT;                                                                      \
+    } while (0)
+
+// ---- launch counters: an event pair around every launch while profiling is enabled
+void prof_flush(State &s) {
+    lq::Prof *p = s.prof;
+    if (!p) return;
+    for (int i = 0; i < p->n; ++i) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, p->ev[2 * i], p->ev[2 * i + 1]) == cudaSuccess) {
+            p->ms[p->cls[i]] += ms;
+            p->launches[p->cls[i]] += 1;
+        } else {
+            (void)cudaGetLastError();
+        }
+    }
+    p->n = 0;
+}
+cudaError_t sync_stream(State &s) {
+    cudaError_t e = cudaStreamSynchronize(s.stream);
+    if (e == cudaSuccess) prof_flush(s);
+    return e;
+}
+int prof_begin(State &s) {
+    lq::Prof *p = s.prof;
+    if (!p) return -1;
+    if (p->n == lq::kProfPool) {
+        if (cudaStreamSynchronize(s.stream) != cudaSuccess) return -1;
+        prof_flush(s);
+    }
+    cudaEventRecord(p->ev[2 * p->n], s.stream);
+    return p->n;
+}
+void prof_end(State &s, int slot, int cls) {
+    lq::Prof *p = s.prof;
+    if (!p || slot < 0) return;
+    cudaEventRecord(p->ev[2 * slot + 1], s.stream);
+    p->cls[slot] = cls;
+    p->n = slot + 1;
+}
+void prof_free(State &s) {
+    if (!s.prof) return;
+    for (int i = 0; i < 2 * lq::kProfPool; ++i) cudaEventDestroy(s.prof->ev[i]);
+    delete s.prof;
+    s.prof = nullptr;
+}
+
+double eps_of(const State &s) { return s.precision == LQ_PRECISION_F64 ? 2.220446049250313e-16 : 1.1920928955078125e-07; }
+
+void free_state(State *s) {
+    if (!s) return;
+    prof_free(*s);
+    for (int i = 0; i < 3; ++i)
+        if (s->U[i]) cudaFree(s->U[i]);
+    if (s->E) cudaFree(s->E);
+    if (s->G) cudaFree(s->G);
+    if (s->partial) cudaFree(s->partial);
+    if (s->d_out) cudaFree(s->d_out);
+    if (s->h_out) cudaFreeHost(s->h_out);
+    if (s->staging) cudaFree(s->staging);
+    delete static_cast<lq_state *>(s);
+}
+
+int ensure_staging(State &s, size_t bytes) {
+    if (s.staging_bytes >= bytes) return LQ_OK;
+    if (s.staging) {
+        LQ_CK(sync_stream(s));
+        LQ_CK(cudaFree(s.staging));
+        s.staging = nullptr;
+        s.staging_bytes = 0;
+    }
+    LQ_CK(cudaMalloc(&s.staging, bytes));
+    s.staging_bytes = bytes;
+    return LQ_OK;
+}
+
+void state_changed(State &s) {
+    s.hu_valid = 0;
+    s.has_pending = 0;
+    s.pending_buf = -1;
+}
+
+int other_buffer(const State &s, int avoid1, int avoid2) {
+    for (int i = 0; i < 3; ++i)
+        if (i != avoid1 && i != avoid2) return i;
+    return -1;
+}
+
+// d_out[offset..offset+2] <- plaquette sums of links buffer U
+int plaquette_sums(State &s, const void *U, int offset) {
+    uint32_t n = 0;
+    LQ_LAUNCH(s, LQ_KERNEL_PLAQUETTE, s.ops->plaquette(s, U, &n));
+    LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->finalize(s, 3, n, offset));
+    return LQ_OK;
+}
+// d_out[offset] <- sum of e^2
+int efield_sumsq(State &s, int offset) {
+    uint32_t n = 0;
+    LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->efield_sumsq(s, &n));
+    LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->finalize(s, 1, n, offset));
+    return LQ_OK;
+}
+int fetch_out(State &s, int count) {
+    LQ_CK(cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * count, cudaMemcpyDeviceToHost, s.stream));
+    LQ_CK(sync_stream(s));
+    return LQ_OK;
+}
+
+// symplectic_n from U[src] (kept) into another buffer; returns the final buffer index.
+// E <- E + dt/2 F(U_k) (+ dt/2 F(U_k) of the next step) ...; U_{k+1} = U_k + dt dU(E, U_k)
+int run_symplectic(State &s, int src, int avoid, double dt, int n, int *final_buf) {
+    int a = other_buffer(s, src, avoid);
+    int b = other_buffer(s, src, a);
+    if (avoid >= 0 && b == avoid) b = src; // only two buffers usable: ping-pong through src
+    const int KD = lq::MD_KICK | lq::MD_DRIFT;
+    LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[src], s.U[a], KD, 0.0, dt / 2.0, dt));
+    int cur = a, nxt = b;
+    for (int i = 1; i < n; ++i) {
+        LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[cur], s.U[nxt], KD, dt / 2.0, dt / 2.0, dt));
+        const int t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[cur], s.U[cur], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+    *final_buf = cur;
+    return LQ_OK;
+}
+
+int project_gauss(State &s, int max_steps, int *steps_done) {
+    const double threshold = eps_of(s) * (double)((uint64_t)s.V * 4 * 8 * 10);
+    const void *U = s.U[s.cur];
+    uint32_t n = 0;
+    int steps = 0;
+    LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+    LQ_LAUNCH(s, LQ_KERNEL_GAUSS_STEP, s.ops->gauss_step(s, U));
+    steps = 1;
+    for (;;) {
+        LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+        LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->finalize(s, 1, n, 0));
+        const int rc = fetch_out(s, 1);
+        if (rc) return rc;
+        const double val_dif = s.h_out[0];
+        if (std::isnan(val_dif)) {
+            if (steps_done) *steps_done = steps;
+            return LQ_ERR_GAUSS_PROJECTION;
+        }
+        if (val_dif <= threshold) break;
+        if (max_steps > 0 && steps + 4 > max_steps) {
+            if (steps_done) *steps_done = steps;
+            return LQ_ERR_NOT_CONVERGED;
+        }
+        for (int k = 0; k < 4; ++k) {
+            if (k) LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+            LQ_LAUNCH(s, LQ_KERNEL_GAUSS_STEP, s.ops->gauss_step(s, U));
+            ++steps;
+        }
+    }
+    if (steps_done) *steps_done = steps;
+    return LQ_OK;
+}
+
+bool valid_std_dev(double sd) { return sd >= 0.0 && !std::isinf(sd); }
+
+} // namespace
+
+extern "C" {
+
+int lq_version(void) { return 100; }
+
+const char *lq_last_error_string(void) { return g_last_error.c_str(); }
+
+const char *lq_status_string(int status) {
+    switch (status) {
+    case LQ_OK: return "ok";
+    case LQ_ERR_NON_POSITIVE_SIZE: return "lattice size must be positive and finite";
+    case LQ_ERR_DIM_TOO_SMALL: return "number of points per direction must be >= 2";
+    case LQ_ERR_ZERO_DIMENSION: return "dimension must be non zero";
+    case LQ_ERR_UNSUPPORTED_DIM: return "dimension must be 2, 3 or 4";
+    case LQ_ERR_INVALID_NORMAL: return "normal distribution N(0, 0.5/beta) is invalid";
+    case LQ_ERR_INCOMPATIBLE_SIZE: return "size of lattice and data are incompatible";
+    case LQ_ERR_GAUSS_PROJECTION: return "gauss projection could not finish";
+    case LQ_ERR_ZERO_INTEGRATION: return "no integration steps";
+    case LQ_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case LQ_ERR_NOT_CONVERGED: return "gauss projection reached its step limit";
+    case LQ_ERR_WRONG_STATE_KIND: return "integration mode does not match the synchronous/leap-frog kind of the state";
+    case LQ_ERR_NO_PENDING: return "no pending HMC proposal";
+    case LQ_ERR_CUDA: return "CUDA error";
+    case LQ_ERR_OUT_OF_MEMORY: return "device out of memory";
+    case LQ_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+int lq_state_create(int dim, int L, double size, double beta, int precision, lq_state **out) {
+    if (!out) return LQ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    // LatticeCyclic::new, src/lattice.rs:190-201
+    if (dim == 0) return LQ_ERR_ZERO_DIMENSION;
+    if (size <= 0.0 || std::isnan(size) || std::isinf(size)) return LQ_ERR_NON_POSITIVE_SIZE;
+    if (L < 2) return LQ_ERR_DIM_TOO_SMALL;
+    if (dim < 2 || dim > 4) return LQ_ERR_UNSUPPORTED_DIM;
+    if (precision != LQ_PRECISION_F64 && precision != LQ_PRECISION_MIXED) return LQ_ERR_INVALID_ARGUMENT;
+    uint64_t V = 1;
+    for (int i = 0; i < dim; ++i) {
+        V *= (uint64_t)L;
+        if (V > (1ull << 28)) return LQ_ERR_INVALID_ARGUMENT; // beyond 32-bit link indexing
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        (void)cudaGetLastError();
+        g_last_error = "no CUDA device visible";
+        return LQ_ERR_NO_DEVICE;
+    }
+    lq_state *s = new (std::nothrow) lq_state();
+    if (!s) return LQ_ERR_OUT_OF_MEMORY;
+    s->dim = dim;
+    s->L = L;
+    s->V = (uint32_t)V;
+    s->size = size;
+    s->beta = beta;
+    s->precision = precision;
+    s->real_bytes = precision == LQ_PRECISION_F64 ? 8 : 4;
+    s->ops = precision == LQ_PRECISION_F64 ? lq::ops_f64(dim) : lq::ops_f32(dim);
+    s->partial_slots = lq::partial_slots_for(s->V);
+    if (s->partial_slots < 1024) s->partial_slots = 1024;
+    int rc = LQ_OK;
+    auto alloc = [&](void **p, size_t bytes, int line) {
+        if (rc) return;
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc", line);
+    };
+    for (int i = 0; i < 3; ++i) alloc(&s->U[i], s->link_bytes(), __LINE__);
+    alloc(&s->E, s->efield_bytes(), __LINE__);
+    alloc(&s->G, s->gauss_bytes(), __LINE__);
+    alloc((void **)&s->partial, sizeof(double) * 3 * (size_t)s->partial_slots, __LINE__);
+    alloc((void **)&s->d_out, sizeof(double) * 16, __LINE__);
+    if (!rc) {
+        cudaError_t e = cudaMallocHost((void **)&s->h_out, sizeof(double) * 16);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaMallocHost", __LINE__);
+    }
+    if (!rc) {
+        cudaError_t e = s->ops->links_cold(*s, s->U[0]);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->E, 0, s->efield_bytes(), s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "state initialisation", __LINE__);
+    }
+    if (rc) {
+        free_state(s);
+        return rc;
+    }
+    *out = s;
+    return LQ_OK;
+}
+
+int lq_state_destroy(lq_state *s) {
+    if (!s) return LQ_OK;
+    cudaStreamSynchronize(s->stream);
+    free_state(s);
+    return LQ_OK;
+}
+
+int lq_state_clone(const lq_state *src, lq_state **out) {
+    if (!src || !out) return LQ_ERR_INVALID_ARGUMENT;
+    lq_state *c = nullptr;
+    int rc = lq_state_create(src->dim, src->L, src->size, src->beta, src->precision, &c);
+    if (rc) return rc;
+    c->stream = src->stream;
+    cudaError_t e = cudaMemcpyAsync(c->U[0], src->U[src->cur], src->link_bytes(), cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->E, src->E, src->efield_bytes(), cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "clone copy", __LINE__);
+        free_state(c);
+        return rc;
+    }
+    c->t = src->t;
+    c->leap = src->leap;
+    c->hu_valid = src->hu_valid;
+    c->hu = src->hu;
+    *out = c;
+    return LQ_OK;
+}
+
+int lq_state_set_stream(lq_state *s, void *stream) {
+    LQ_CHECK_STATE(s);
+    LQ_CK(sync_stream(*s));
+    s->stream = (cudaStream_t)stream;
+    return LQ_OK;
+}
+
+int lq_state_info(const lq_state *s, int *dim, int *L, double *size, double *beta, int *precision,
+                  long long *n_sites, long long *t, int *is_leap) {
+    LQ_CHECK_STATE(s);
+    if (dim) *dim = s->dim;
+    if (L) *L = s->L;
+    if (size) *size = s->size;
+    if (beta) *beta = s->beta;
+    if (precision) *precision = s->precision;
+    if (n_sites) *n_sites = (long long)s->V;
+    if (t) *t = s->t;
+    if (is_leap) *is_leap = s->leap;
+    return LQ_OK;
+}
+
+int lq_state_set_beta(lq_state *s, double beta) {
+    LQ_CHECK_STATE(s);
+    s->beta = beta;
+    s->hu_valid = 0;
+    s->has_pending = 0;
+    return LQ_OK;
+}
+
+int lq_state_device_bytes(const lq_state *s, size_t *bytes) {
+    LQ_CHECK_STATE(s);
+    if (!bytes) return LQ_ERR_INVALID_ARGUMENT;
+    *bytes = 3 * s->link_bytes() + s->efield_bytes() + s->gauss_bytes() +
+             sizeof(double) * (3 * (size_t)s->partial_slots + 16) + s->staging_bytes;
+    return LQ_OK;
+}
+
+// ------------------------------------------------------------------ fields
+int lq_links_upload(lq_state *s, const double *links, size_t n) {
+    LQ_CHECK_STATE(s);
+    if (!links) return LQ_ERR_INVALID_ARGUMENT;
+    if (n != (size_t)s->V * s->dim * 18) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n * sizeof(double);
+    int rc = ensure_staging(*s, bytes);
+    if (rc) return rc;
+    LQ_CK(cudaMemcpyAsync(s->staging, links, bytes, cudaMemcpyHostToDevice, s->stream));
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->links_from_aos(*s, (const double *)s->staging, s->U[s->cur]));
+    LQ_CK(sync_stream(*s));
+    state_changed(*s);
+    return LQ_OK;
+}
+
+int lq_links_download(lq_state *s, double *links, size_t n) {
+    LQ_CHECK_STATE(s);
+    if (!links) return LQ_ERR_INVALID_ARGUMENT;
+    if (n != (size_t)s->V * s->dim * 18) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n * sizeof(double);
+    int rc = ensure_staging(*s, bytes);
+    if (rc) return rc;
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->links_to_aos(*s, s->U[s->cur], (double *)s->staging));
+    LQ_CK(cudaMemcpyAsync(links, s->staging, bytes, cudaMemcpyDeviceToHost, s->stream));
+    LQ_CK(sync_stream(*s));
+    return LQ_OK;
+}
+
+int lq_links_set_cold(lq_state *s) {
+    LQ_CHECK_STATE(s);
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->links_cold(*s, s->U[s->cur]));
+    LQ_CK(sync_stream(*s));
+    state_changed(*s);
+    return LQ_OK;
+}
+
+int lq_links_random(lq_state *s, uint64_t seed) {
+    LQ_CHECK_STATE(s);
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->links_random(*s, s->U[s->cur], seed));
+    LQ_CK(sync_stream(*s));
+    state_changed(*s);
+    return LQ_OK;
+}
+
+int lq_efield_upload(lq_state *s, const double *efield, size_t n) {
+    LQ_CHECK_STATE(s);
+    if (!efield) return LQ_ERR_INVALID_ARGUMENT;
+    if (n != (size_t)s->V * s->dim * 8) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n * sizeof(double);
+    int rc = ensure_staging(*s, bytes);
+    if (rc) return rc;
+    LQ_CK(cudaMemcpyAsync(s->staging, efield, bytes, cudaMemcpyHostToDevice, s->stream));
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_from_aos(*s, (const double *)s->staging));
+    LQ_CK(sync_stream(*s));
+    s->has_pending = 0;
+    return LQ_OK;
+}
+
+int lq_efield_download(lq_state *s, double *efield, size_t n) {
+    LQ_CHECK_STATE(s);
+    if (!efield) return LQ_ERR_INVALID_ARGUMENT;
+    if (n != (size_t)s->V * s->dim * 8) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n * sizeof(double);
+    int rc = ensure_staging(*s, bytes);
+    if (rc) return rc;
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_to_aos(*s, (double *)s->staging));
+    LQ_CK(cudaMemcpyAsync(efield, s->staging, bytes, cudaMemcpyDeviceToHost, s->stream));
+    LQ_CK(sync_stream(*s));
+    return LQ_OK;
+}
+
+int lq_efield_set_cold(lq_state *s) {
+    LQ_CHECK_STATE(s);
+    LQ_CK(cudaMemsetAsync(s->E, 0, s->efield_bytes(), s->stream));
+    LQ_CK(sync_stream(*s));
+    s->has_pending = 0;
+    return LQ_OK;
+}
+
+int lq_efield_random_normal(lq_state *s, uint64_t seed, uint64_t counter, double std_dev) {
+    LQ_CHECK_STATE(s);
+    if (!valid_std_dev(std_dev)) return LQ_ERR_INVALID_NORMAL;
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_normal(*s, seed, counter, std_dev));
+    LQ_CK(sync_stream(*s));
+    s->has_pending = 0;
+    return LQ_OK;
+}
+
+// ------------------------------------------------------------------ observables
+int lq_hamiltonian_links(lq_state *s, double *out) {
+    LQ_CHECK_STATE(s);
+    if (!out) return LQ_ERR_INVALID_ARGUMENT;
+    if (!s->hu_valid) {
+        int rc = plaquette_sums(*s, s->U[s->cur], 0);
+        if (!rc) rc = fetch_out(*s, 3);
+        if (rc) return rc;
+        s->hu = s->h_out[0] * s->beta;
+        s->hu_valid = 1;
+    }
+    *out = s->hu;
+    return LQ_OK;
+}
+
+int lq_hamiltonian_efield(lq_state *s, double *out) {
+    LQ_CHECK_STATE(s);
+    if (!out) return LQ_ERR_INVALID_ARGUMENT;
+    int rc = efield_sumsq(*s, 0);
+    if (!rc) rc = fetch_out(*s, 1);
+    if (rc) return rc;
+    *out = s->h_out[0] / 2.0 * s->beta;
+    return LQ_OK;
+}
+
+int lq_hamiltonian_total(lq_state *s, double *out) {
+    LQ_CHECK_STATE(s);
+    if (!out) return LQ_ERR_INVALID_ARGUMENT;
+    double hu = 0.0, he = 0.0;
+    int rc = lq_hamiltonian_links(s, &hu);
+    if (!rc) rc = lq_hamiltonian_efield(s, &he);
+    if (rc) return rc;
+    *out = hu + he;
+    return LQ_OK;
+}
+
+int lq_average_trace_plaquette(lq_state *s, double *re, double *im) {
+    LQ_CHECK_STATE(s);
+    int rc = plaquette_sums(*s, s->U[s->cur], 0);
+    if (!rc) rc = fetch_out(*s, 3);
+    if (rc) return rc;
+    const double n_plaq = (double)((uint64_t)s->V * (uint64_t)((s->dim * (s->dim - 1)) / 2));
+    if (re) *re = s->h_out[1] / n_plaq;
+    if (im) *im = s->h_out[2] / n_plaq;
+    s->hu = s->h_out[0] * s->beta;
+    s->hu_valid = 1;
+    return LQ_OK;
+}
+
+int lq_gauss_sum_div(lq_state *s, double *out) {
+    LQ_CHECK_STATE(s);
+    if (!out) return LQ_ERR_INVALID_ARGUMENT;
+    uint32_t n = 0;
+    LQ_LAUNCH(*s, LQ_KERNEL_GAUSS, s->ops->gauss(*s, s->U[s->cur], &n));
+    LQ_LAUNCH(*s, LQ_KERNEL_REDUCE, s->ops->finalize(*s, 1, n, 0));
+    int rc = fetch_out(*s, 1);
+    if (rc) return rc;
+    *out = s->h_out[0];
+    return LQ_OK;
+}
+
+int lq_gauss_download(lq_state *s, double *out, size_t n_doubles) {
+    LQ_CHECK_STATE(s);
+    if (!out) return LQ_ERR_INVALID_ARGUMENT;
+    if (n_doubles != (size_t)s->V * 8) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n_doubles * sizeof(double);
+    int rc = ensure_staging(*s, bytes);
+    if (rc) return rc;
+    uint32_t n = 0;
+    LQ_LAUNCH(*s, LQ_KERNEL_GAUSS, s->ops->gauss(*s, s->U[s->cur], &n));
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->gauss_to_aos(*s, (double *)s->staging));
+    LQ_CK(cudaMemcpyAsync(out, s->staging, bytes, cudaMemcpyDeviceToHost, s->stream));
+    LQ_CK(sync_stream(*s));
+    return LQ_OK;
+}
+
+// ------------------------------------------------------------------ updates
+int lq_project_gauss(lq_state *s, int max_steps, int *steps_done) {
+    LQ_CHECK_STATE(s);
+    s->has_pending = 0;
+    return project_gauss(*s, max_steps, steps_done);
+}
+
+int lq_normalize_link_matrices(lq_state *s) {
+    LQ_CHECK_STATE(s);
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->normalize(*s, s->U[s->cur]));
+    LQ_CK(sync_stream(*s));
+    state_changed(*s);
+    return LQ_OK;
+}
+
+int lq_integrate(lq_state *s, int mode, double dt, int n) {
+    LQ_CHECK_STATE(s);
+    if (mode < LQ_SYNC_SYNC || mode > LQ_SYMPLECTIC) return LQ_ERR_INVALID_ARGUMENT;
+    if (n <= 0) return LQ_ERR_ZERO_INTEGRATION;
+    const bool needs_leap = (mode == LQ_LEAP_LEAP || mode == LQ_LEAP_SYNC);
+    if ((needs_leap && !s->leap) || (!needs_leap && s->leap)) return LQ_ERR_WRONG_STATE_KIND;
+    if ((mode == LQ_SYNC_LEAP || mode == LQ_LEAP_SYNC) && n != 1) return LQ_ERR_WRONG_STATE_KIND;
+    State &st = *s;
+    state_changed(st);
+    const int KD = lq::MD_KICK | lq::MD_DRIFT;
+    int a = st.cur, b = other_buffer(st, st.cur, -1);
+    switch (mode) {
+    case LQ_SYNC_SYNC:
+        for (int i = 0; i < n; ++i) {
+            LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], KD | lq::MD_DRIFT_OLD_E, 0.0, dt, dt));
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        st.cur = a;
+        st.t += n;
+        break;
+    case LQ_SYNC_LEAP:
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[a], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+        st.leap = 1;
+        break;
+    case LQ_LEAP_LEAP:
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], lq::MD_DRIFT, 0.0, 0.0, dt));
+        for (int i = 1; i < n; ++i) {
+            LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[a], KD, 0.0, dt, dt));
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], lq::MD_KICK, 0.0, dt, 0.0));
+        st.cur = b;
+        st.t += n;
+        break;
+    case LQ_LEAP_SYNC:
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], lq::MD_DRIFT, 0.0, 0.0, dt));
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+        st.cur = b;
+        st.leap = 0;
+        st.t += 1;
+        break;
+    default: { // LQ_SYMPLECTIC
+        int fin = -1;
+        int rc = run_symplectic(st, st.cur, -1, dt, n, &fin);
+        if (rc) return rc;
+        st.cur = fin;
+        st.t += n;
+        break;
+    }
+    }
+    LQ_CK(sync_stream(st));
+    return LQ_OK;
+}
+
+int lq_leapfrog_n(lq_state *s, double dt, int n) {
+    LQ_CHECK_STATE(s);
+    if (n <= 0) return LQ_ERR_ZERO_INTEGRATION;
+    if (s->leap) return LQ_ERR_WRONG_STATE_KIND;
+    State &st = *s;
+    state_changed(st);
+    const int KD = lq::MD_KICK | lq::MD_DRIFT;
+    int a = st.cur, b = other_buffer(st, st.cur, -1);
+    // sync -> leap: E += dt/2 F(U0)
+    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[a], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+    // first drift (of leap_leap, or of leap_sync when n == 1)
+    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], lq::MD_DRIFT, 0.0, 0.0, dt));
+    for (int i = 1; i < n; ++i) {
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[a], KD, 0.0, dt, dt));
+        const int t = a;
+        a = b;
+        b = t;
+    }
+    // leap -> sync: E += dt/2 F(U_n)
+    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+    st.cur = b;
+    st.t += n;
+    LQ_CK(sync_stream(st));
+    return LQ_OK;
+}
+
+// ------------------------------------------------------------------ HMC
+int lq_hmc_refresh(lq_state *s, uint64_t seed, uint64_t counter, int max_gauss_steps, int *gauss_steps) {
+    LQ_CHECK_STATE(s);
+    const double sd = 0.5 / s->beta;
+    if (!valid_std_dev(sd)) return LQ_ERR_INVALID_NORMAL;
+    s->has_pending = 0;
+    s->leap = 0;
+    s->t = 0;
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_normal(*s, seed, counter, sd));
+    return project_gauss(*s, max_gauss_steps, gauss_steps);
+}
+
+int lq_hmc_refresh_upload(lq_state *s, const double *efield_raw, size_t n, int max_gauss_steps, int *gauss_steps) {
+    LQ_CHECK_STATE(s);
+    if (!valid_std_dev(0.5 / s->beta)) return LQ_ERR_INVALID_NORMAL;
+    int rc = lq_efield_upload(s, efield_raw, n);
+    if (rc) return rc;
+    s->leap = 0;
+    s->t = 0;
+    return project_gauss(*s, max_gauss_steps, gauss_steps);
+}
+
+int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_old, double *h_new) {
+    LQ_CHECK_STATE(s);
+    if (n_steps <= 0) return LQ_ERR_ZERO_INTEGRATION;
+    if (s->leap) return LQ_ERR_WRONG_STATE_KIND;
+    State &st = *s;
+    st.has_pending = 0;
+    int rc = LQ_OK;
+    // H of the start state: d_out[0..2] plaquette sums (unless cached), d_out[3] sum e^2
+    if (!st.hu_valid) {
+        rc = plaquette_sums(st, st.U[st.cur], 0);
+        if (rc) return rc;
+    }
+    rc = efield_sumsq(st, 3);
+    if (rc) return rc;
+    int fin = -1;
+    rc = run_symplectic(st, st.cur, -1, dt, n_steps, &fin);
+    if (rc) return rc;
+    // H of the proposal: d_out[4..6], d_out[7]
+    rc = plaquette_sums(st, st.U[fin], 4);
+    if (!rc) rc = efield_sumsq(st, 7);
+    if (!rc) rc = fetch_out(st, 8);
+    if (rc) return rc;
+    const double hu_old = st.hu_valid ? st.hu : st.h_out[0] * st.beta;
+    const double he_old = st.h_out[3] / 2.0 * st.beta;
+    const double hu_new = st.h_out[4] * st.beta;
+    const double he_new = st.h_out[7] / 2.0 * st.beta;
+    const double h0 = hu_old + he_old, h1 = hu_new + he_new;
+    // probability_of_replacement, hybrid_monte_carlo.rs:584-589 (NaN clamps to 1 as f64::min does)
+    double p = std::fmax(std::fmin(std::exp(h0 - h1), 1.0), 0.0);
+    if (prob) *prob = p;
+    if (h_old) *h_old = h0;
+    if (h_new) *h_new = h1;
+    st.hu = hu_old;
+    st.hu_valid = 1;
+    st.pending_hu_old = hu_old;
+    st.pending_hu_new = hu_new;
+    st.pending_buf = fin;
+    st.has_pending = 1;
+    st.t = n_steps;
+    return LQ_OK;
+}
+
+int lq_hmc_decide(lq_state *s, int accept) {
+    LQ_CHECK_STATE(s);
+    if (!s->has_pending) return LQ_ERR_NO_PENDING;
+    if (accept) {
+        s->cur = s->pending_buf;
+        s->hu = s->pending_hu_new;
+    } else {
+        s->hu = s->pending_hu_old;
+    }
+    s->hu_valid = 1;
+    s->has_pending = 0;
+    s->pending_buf = -1;
+    return LQ_OK;
+}
+
+int lq_hmc_trajectory(lq_state *s, double dt, int n_steps, uint64_t seed, uint64_t counter, double uniform,
+                      int max_gauss_steps, int *accepted, double *prob, double *delta_h, int *gauss_steps) {
+    LQ_CHECK_STATE(s);
+    if (n_steps <= 0) return LQ_ERR_ZERO_INTEGRATION;
+    int rc = lq_hmc_refresh(s, seed, counter, max_gauss_steps, gauss_steps);
+    if (rc) return rc;
+    double p = 0.0, h0 = 0.0, h1 = 0.0;
+    rc = lq_hmc_propose(s, dt, n_steps, &p, &h0, &h1);
+    if (rc) return rc;
+    const int acc = (p >= 1.0 || uniform < p) ? 1 : 0;
+    rc = lq_hmc_decide(s, acc);
+    if (rc) return rc;
+    if (accepted) *accepted = acc;
+    if (prob) *prob = p;
+    if (delta_h) *delta_h = h1 - h0;
+    return LQ_OK;
+}
+
+int lq_profile_enable(lq_state *s, int on) {
+    LQ_CHECK_STATE(s);
+    LQ_CK(sync_stream(*s));
+    if (on && !s->prof) {
+        lq::Prof *p = new (std::nothrow) lq::Prof();
+        if (!p) return LQ_ERR_OUT_OF_MEMORY;
+        for (int i = 0; i < 2 * lq::kProfPool; ++i) {
+            cudaError_t e = cudaEventCreate(&p->ev[i]);
+            if (e != cudaSuccess) {
+                for (int j = 0; j < i; ++j) cudaEventDestroy(p->ev[j]);
+                delete p;
+                return cuda_fail(e, "cudaEventCreate", __LINE__);
+            }
+        }
+        s->prof = p;
+    } else if (!on) {
+        prof_free(*s);
+    }
+    return LQ_OK;
+}
+
+int lq_profile_read(lq_state *s, int kernel_class, long long *launches, double *total_ms, int reset) {
+    LQ_CHECK_STATE(s);
+    if (kernel_class < 0 || kernel_class >= LQ_KERNEL_CLASSES) return LQ_ERR_INVALID_ARGUMENT;
+    LQ_CK(sync_stream(*s));
+    if (!s->prof) {
+        if (launches) *launches = 0;
+        if (total_ms) *total_ms = 0.0;
+        return LQ_OK;
+    }
+    if (launches) *launches = s->prof->launches[kernel_class];
+    if (total_ms) *total_ms = s->prof->ms[kernel_class];
+    if (reset) {
+        for (int i = 0; i < lq::kProfClasses; ++i) {
+            s->prof->launches[i] = 0;
+            s->prof->ms[i] = 0.0;
+        }
+    }
+    return LQ_OK;
+}
+
+} // extern "C"

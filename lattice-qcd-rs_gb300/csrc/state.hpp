@@ -1,0 +1,101 @@
+// state.hpp -- the device-resident HMC state behind the lq_state handle, and the
+// per-(D, precision) table of device operations.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "lqgpu.h"
+
+namespace lq {
+
+struct Ops;
+
+// CUDA-event launch counters (lq_profile_enable / lq_profile_read)
+constexpr int kProfPool = 1024;
+constexpr int kProfClasses = 6;
+struct Prof {
+    cudaEvent_t ev[2 * kProfPool];
+    int cls[kProfPool];
+    int n = 0;
+    long long launches[kProfClasses] = {0, 0, 0, 0, 0, 0};
+    double ms[kProfClasses] = {0, 0, 0, 0, 0, 0};
+};
+
+// Buffers are untyped here; the element type is double or float according to `precision`.
+struct State {
+    int dim = 0;
+    int L = 0;
+    uint32_t V = 0;
+    double size = 1.0;
+    double beta = 1.0;
+    int precision = LQ_PRECISION_F64;
+    size_t real_bytes = 8; // sizeof(T)
+    cudaStream_t stream = nullptr;
+
+    void *U[3] = {nullptr, nullptr, nullptr}; // link buffers (SoA); U[cur] is the state
+    int cur = 0;
+    void *E = nullptr;   // E-field (SoA)
+    void *G = nullptr;   // Gauss-law coefficients, 8 per site
+    double *partial = nullptr;
+    uint32_t partial_slots = 0; // slots per row of `partial`
+    double *d_out = nullptr;    // device scalars
+    double *h_out = nullptr;    // pinned host mirror of d_out
+    void *staging = nullptr;    // f64 AoS staging for uploads/downloads
+    size_t staging_bytes = 0;
+
+    long long t = 0;
+    int leap = 0;
+
+    // HMC proposal bookkeeping
+    int has_pending = 0;
+    int pending_buf = -1;
+    double pending_hu_old = 0.0, pending_hu_new = 0.0;
+    // cached hamiltonian_links of U[cur] (reductions are deterministic, so the cached value
+    // equals a recomputation)
+    int hu_valid = 0;
+    double hu = 0.0;
+
+    const Ops *ops = nullptr;
+    Prof *prof = nullptr; // non-null while profiling is enabled
+
+    size_t link_elems() const { return (size_t)V * dim * 9; }   // complex elements
+    size_t link_bytes() const { return link_elems() * 2 * real_bytes; }
+    size_t efield_elems() const { return (size_t)V * dim * 8; } // reals
+    size_t efield_bytes() const { return efield_elems() * real_bytes; }
+    size_t gauss_bytes() const { return (size_t)V * 8 * real_bytes; }
+};
+
+// Device operations of one (D, T) instantiation.  Launches are asynchronous on s.stream
+// and return cudaError_t of the launch.
+struct Ops {
+    cudaError_t (*links_from_aos)(State &s, const double *d_aos, void *dst);
+    cudaError_t (*links_to_aos)(State &s, const void *src, double *d_aos);
+    cudaError_t (*links_cold)(State &s, void *dst);
+    cudaError_t (*links_random)(State &s, void *dst, uint64_t seed);
+    cudaError_t (*efield_from_aos)(State &s, const double *d_aos);
+    cudaError_t (*efield_to_aos)(State &s, double *d_aos);
+    cudaError_t (*efield_normal)(State &s, uint64_t seed, uint64_t counter, double sd);
+    // md: mode bits MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E; h1, h2 kick step sizes; dt drift step
+    cudaError_t (*md)(State &s, const void *Uin, void *Uout, int mode, double h1, double h2, double dt);
+    // gauss: G <- gauss(E, U), residual partials into s.partial (row 0), returns #partials
+    cudaError_t (*gauss)(State &s, const void *U, uint32_t *n_partials);
+    cudaError_t (*gauss_step)(State &s, const void *U);
+    cudaError_t (*gauss_to_aos)(State &s, double *d_out);
+    // plaquette partials (3 rows) of links buffer U, returns #partials
+    cudaError_t (*plaquette)(State &s, const void *U, uint32_t *n_partials);
+    cudaError_t (*efield_sumsq)(State &s, uint32_t *n_partials);
+    cudaError_t (*normalize)(State &s, void *U);
+    // finalize NV rows of n partials into d_out[offset..]
+    cudaError_t (*finalize)(State &s, int nv, uint32_t n, int offset);
+};
+
+const Ops *ops_f64(int dim);
+const Ops *ops_f32(int dim);
+
+// partial slots needed for V sites
+inline uint32_t partial_slots_for(uint32_t V) { return (V + 127) / 128 + 64; }
+
+} // namespace lq
+
+struct lq_state : public lq::State {};

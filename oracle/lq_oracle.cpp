@@ -1,0 +1,886 @@
+/*
+ * lq_oracle.cpp -- CPU oracle for the HMC molecular-dynamics path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA library and the CPU baseline
+ * of bench.py.  Nothing in the product path links or calls this file.
+ *
+ * A C++17 restatement of lattice-qcd-rs v0.2.1 (Rust).  Each routine names the
+ * reference file:line it follows.  Loop orders, the array-of-structures f64 layout,
+ * the per-step allocation of new fields and the operation order inside each
+ * formula follow the reference, so that this code is both the parity oracle and a
+ * fair stand-in for the reference's CPU cost.  OpenMP parallel loops over sites and
+ * links stand in for rayon's `par_iter`/`par_bridge` (src/thread.rs:684-699).
+ *
+ * Third-party arithmetic restated here (sources not vendored in the reference):
+ *  - nalgebra 0.31 3x3 complex products, adjoint, trace, determinant, cross,
+ *    try_normalize (src/su3.rs:279-309);
+ *  - num-complex textbook complex product;
+ *  - rand 0.8 `Uniform<f64>` (53-bit mantissa fill, value0_1 * scale + low) and
+ *    `Bernoulli` (p == 1 always true, else u < p);
+ *  - Xoshiro256++ / SplitMix64 (Blackman & Vigna) as the seeded generator;
+ *  - normals: Box-Muller over the Xoshiro uniforms.  rand_distr's ziggurat is NOT
+ *    restated, so random streams are not bit-identical to the Rust crate (parity
+ *    of random streams is unpinned); parity tests inject the same buffers into this
+ *    oracle and the CUDA library instead.
+ *
+ * Compiled with -ffp-contract=off so no multiply-add is fused (Rust never fuses),
+ * giving identical results on x86-64 and aarch64.
+ */
+#include "lq_oracle.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <array>
+#include <omp.h>
+
+namespace {
+
+constexpr double F64_EPS = 2.220446049250313e-16; /* f64::EPSILON */
+
+struct Cx {
+    double re, im;
+};
+inline Cx cx(double r, double i = 0.0) { return Cx{r, i}; }
+inline Cx operator+(Cx a, Cx b) { return Cx{a.re + b.re, a.im + b.im}; }
+inline Cx operator-(Cx a, Cx b) { return Cx{a.re - b.re, a.im - b.im}; }
+/* num-complex Mul: (a.re*b.re - a.im*b.im, a.re*b.im + a.im*b.re) */
+inline Cx operator*(Cx a, Cx b) { return Cx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+inline Cx conj(Cx a) { return Cx{a.re, -a.im}; }
+inline double modulus(Cx a) { return std::hypot(a.re, a.im); }
+inline double modulus_squared(Cx a) { return a.re * a.re + a.im * a.im; }
+
+/* 3x3 complex matrix, m[row][col] */
+struct M3 {
+    Cx m[3][3];
+};
+
+inline M3 zero3() {
+    M3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = cx(0.0, 0.0);
+    return r;
+}
+inline M3 identity3() {
+    M3 r = zero3();
+    for (int i = 0; i < 3; ++i) r.m[i][i] = cx(1.0, 0.0);
+    return r;
+}
+/* nalgebra gemm for 3x3: result column j = sum_k a.col(k) * b[k][j], k ascending */
+inline M3 operator*(const M3 &a, const M3 &b) {
+    M3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            Cx s = a.m[i][0] * b.m[0][j];
+            s = s + a.m[i][1] * b.m[1][j];
+            s = s + a.m[i][2] * b.m[2][j];
+            r.m[i][j] = s;
+        }
+    return r;
+}
+inline M3 operator+(const M3 &a, const M3 &b) {
+    M3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] + b.m[i][j];
+    return r;
+}
+inline M3 operator-(const M3 &a, const M3 &b) {
+    M3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] - b.m[i][j];
+    return r;
+}
+/* matrix * complex scalar (element * scalar) */
+inline M3 operator*(const M3 &a, Cx c) {
+    M3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] * c;
+    return r;
+}
+inline M3 adjoint(const M3 &a) {
+    M3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = conj(a.m[j][i]);
+    return r;
+}
+inline Cx trace(const M3 &a) { return a.m[0][0] + a.m[1][1] + a.m[2][2]; }
+
+/* nalgebra 3x3 determinant (cofactor expansion along the first row) */
+inline Cx determinant(const M3 &a) {
+    const Cx m11 = a.m[0][0], m12 = a.m[0][1], m13 = a.m[0][2];
+    const Cx m21 = a.m[1][0], m22 = a.m[1][1], m23 = a.m[1][2];
+    const Cx m31 = a.m[2][0], m32 = a.m[2][1], m33 = a.m[2][2];
+    const Cx minor_m12_m23 = m22 * m33 - m32 * m23;
+    const Cx minor_m11_m23 = m21 * m33 - m31 * m23;
+    const Cx minor_m11_m22 = m21 * m32 - m31 * m22;
+    return m11 * minor_m12_m23 - m12 * minor_m11_m23 + m13 * minor_m11_m22;
+}
+
+/* serde layout <-> M3: 18 doubles, column-major, (re, im) */
+inline M3 load_m3(const double *p) {
+    M3 r;
+    for (int c = 0; c < 3; ++c)
+        for (int row = 0; row < 3; ++row) r.m[row][c] = cx(p[(c * 3 + row) * 2], p[(c * 3 + row) * 2 + 1]);
+    return r;
+}
+inline void store_m3(const M3 &a, double *p) {
+    for (int c = 0; c < 3; ++c)
+        for (int row = 0; row < 3; ++row) {
+            p[(c * 3 + row) * 2] = a.m[row][c].re;
+            p[(c * 3 + row) * 2 + 1] = a.m[row][c].im;
+        }
+}
+
+/* ---- su(3) generators T^a = lambda^a / 2, src/su3.rs:24-194 ---- */
+constexpr double MINUS_ONE_OVER_SQRT_3 = -0.5773502691896258;
+constexpr double ONE_OVER_2_SQRT_3 = 0.2886751345948129;
+
+M3 make_generator(int a) {
+    M3 g = zero3();
+    switch (a) {
+    case 0: g.m[0][1] = cx(0.5); g.m[1][0] = cx(0.5); break;
+    case 1: g.m[0][1] = cx(0.0, -0.5); g.m[1][0] = cx(0.0, 0.5); break;
+    case 2: g.m[0][0] = cx(0.5); g.m[1][1] = cx(-0.5); break;
+    case 3: g.m[0][2] = cx(0.5); g.m[2][0] = cx(0.5); break;
+    case 4: g.m[0][2] = cx(0.0, -0.5); g.m[2][0] = cx(0.0, 0.5); break;
+    case 5: g.m[1][2] = cx(0.5); g.m[2][1] = cx(0.5); break;
+    case 6: g.m[1][2] = cx(0.0, -0.5); g.m[2][1] = cx(0.0, 0.5); break;
+    default:
+        g.m[0][0] = cx(ONE_OVER_2_SQRT_3);
+        g.m[1][1] = cx(ONE_OVER_2_SQRT_3);
+        g.m[2][2] = cx(MINUS_ONE_OVER_SQRT_3);
+        break;
+    }
+    return g;
+}
+
+struct Generators {
+    M3 g[8];
+    M3 sum; /* GENERATORS.iter().sum(), used by gauss_sum_div (src/field.rs:1212) */
+    Generators() {
+        M3 s = zero3();
+        for (int a = 0; a < 8; ++a) {
+            g[a] = make_generator(a);
+            s = s + g[a];
+        }
+        sum = s;
+    }
+};
+const Generators &gens() {
+    static const Generators G;
+    return G;
+}
+
+/* Su3Adjoint::to_matrix, src/field.rs:106-112: sum_a T^a * e^a, folded from zero */
+inline M3 to_matrix(const double *e8) {
+    const Generators &G = gens();
+    M3 r = zero3();
+    for (int a = 0; a < 8; ++a) r = r + G.g[a] * cx(e8[a]);
+    return r;
+}
+/* Su3Adjoint::trace_squared, src/field.rs:164-167 */
+inline double trace_squared(const double *e8) {
+    double s = 0.0;
+    for (int a = 0; a < 8; ++a) s = s + e8[a] * e8[a];
+    return s / 2.0;
+}
+
+/* 1/n! with n! held exactly (u128 in the reference, src/su3.rs:750-775) */
+double inv_factorial(int n) {
+    unsigned __int128 f = 1;
+    for (int i = 2; i <= n; ++i) f *= (unsigned __int128)i;
+    return 1.0 / (double)f;
+}
+
+/* su3_exp_i, src/su3.rs:832-855 (Cayley-Hamilton, N = 26) */
+M3 su3_exp_i(const double *adj) {
+    const int N_LOOP = 25;
+    const Cx I = cx(0.0, 1.0);
+    Cx q0 = cx(inv_factorial(N_LOOP));
+    Cx q1 = cx(0.0), q2 = cx(0.0);
+    const M3 m = to_matrix(adj);
+    const Cx d = determinant(m) * I;
+    const Cx t = cx(-0.5 * trace_squared(adj));
+    for (int i = N_LOOP - 1; i >= 0; --i) {
+        const Cx q0_n = cx(inv_factorial(i)) + d * q2;
+        const Cx q1_n = I * (q0 - t * q2);
+        const Cx q2_n = I * q1;
+        q0 = q0_n;
+        q1 = q1_n;
+        q2 = q2_n;
+    }
+    M3 diag = zero3();
+    for (int i = 0; i < 3; ++i) diag.m[i][i] = q0;
+    return diag + m * q1 + (m * m) * q2;
+}
+
+/* su3_exp_r, src/su3.rs:916-938 */
+M3 su3_exp_r(const double *adj) {
+    const int N_LOOP = 25;
+    const Cx I = cx(0.0, 1.0);
+    Cx q0 = cx(inv_factorial(N_LOOP));
+    Cx q1 = cx(0.0), q2 = cx(0.0);
+    const M3 m = to_matrix(adj);
+    const Cx d = determinant(m) * I;
+    const Cx t = cx(-0.5 * trace_squared(adj));
+    for (int i = N_LOOP - 1; i >= 0; --i) {
+        const Cx q0_n = cx(inv_factorial(i)) - (I * d) * q2;
+        const Cx q1_n = q0 - t * q2;
+        const Cx q2_n = q1;
+        q0 = q0_n;
+        q1 = q1_n;
+        q2 = q2_n;
+    }
+    M3 diag = zero3();
+    for (int i = 0; i < 3; ++i) diag.m[i][i] = q0;
+    return diag + m * q1 + (m * m) * q2;
+}
+
+/* ---- vectors for Gram-Schmidt, src/su3.rs:279-309 ---- */
+struct V3 {
+    Cx v[3];
+};
+inline double norm(const V3 &a) {
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) s = s + modulus_squared(a.v[i]);
+    return std::sqrt(s);
+}
+/* nalgebra try_normalize(eps): None when the norm <= eps */
+inline bool try_normalize(const V3 &a, double eps, V3 &out) {
+    const double n = norm(a);
+    if (n <= eps) return false;
+    for (int i = 0; i < 3; ++i) out.v[i] = cx(a.v[i].re / n, a.v[i].im / n);
+    return true;
+}
+/* non-conjugating dot: sum_i a_i * b_i */
+inline Cx dot(const V3 &a, const V3 &b) {
+    Cx s = a.v[0] * b.v[0];
+    s = s + a.v[1] * b.v[1];
+    s = s + a.v[2] * b.v[2];
+    return s;
+}
+inline V3 conjv(const V3 &a) {
+    V3 r;
+    for (int i = 0; i < 3; ++i) r.v[i] = conj(a.v[i]);
+    return r;
+}
+inline V3 cross(const V3 &a, const V3 &b) {
+    V3 r;
+    r.v[0] = a.v[1] * b.v[2] - a.v[2] * b.v[1];
+    r.v[1] = a.v[2] * b.v[0] - a.v[0] * b.v[2];
+    r.v[2] = a.v[0] * b.v[1] - a.v[1] * b.v[0];
+    return r;
+}
+/* create_matrix_from_2_vector, src/su3.rs:279-287: columns [v1, v2, conj(v1) x conj(v2)] */
+M3 create_matrix_from_2_vector(const V3 &v1, const V3 &v2) {
+    const V3 c = cross(conjv(v1), conjv(v2));
+    M3 r;
+    for (int i = 0; i < 3; ++i) {
+        r.m[i][0] = v1.v[i];
+        r.m[i][1] = v2.v[i];
+        r.m[i][2] = c.v[i];
+    }
+    return r;
+}
+/* ortho_matrix_from_2_vector, src/su3.rs:290-295 */
+M3 ortho_matrix_from_2_vector(const V3 &v1, const V3 &v2) {
+    V3 v1_new;
+    if (!try_normalize(v1, F64_EPS, v1_new)) v1_new = v1;
+    const Cx proj = dot(conjv(v1_new), v2);
+    V3 v2_temp;
+    for (int i = 0; i < 3; ++i) v2_temp.v[i] = v2.v[i] - v1_new.v[i] * proj;
+    V3 v2_new;
+    if (!try_normalize(v2_temp, F64_EPS, v2_new)) v2_new = v2_temp;
+    return create_matrix_from_2_vector(v1_new, v2_new);
+}
+/* orthonormalize_matrix, src/su3.rs:298-303 */
+M3 orthonormalize_matrix(const M3 &m) {
+    V3 v1, v2;
+    for (int i = 0; i < 3; ++i) {
+        v1.v[i] = m.m[i][0];
+        v2.v[i] = m.m[i][1];
+    }
+    return ortho_matrix_from_2_vector(v1, v2);
+}
+
+/* ---- random numbers ---- */
+struct Rng {
+    uint64_t s[4];
+    bool has_spare = false;
+    double spare = 0.0;
+};
+inline uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+uint64_t splitmix64(uint64_t &x) {
+    uint64_t z = (x += 0x9e3779b97f4a7c15ULL);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+uint64_t next_u64(Rng &r) {
+    const uint64_t result = rotl(r.s[0] + r.s[3], 23) + r.s[0];
+    const uint64_t t = r.s[1] << 17;
+    r.s[2] ^= r.s[0];
+    r.s[3] ^= r.s[1];
+    r.s[1] ^= r.s[2];
+    r.s[0] ^= r.s[3];
+    r.s[2] ^= t;
+    r.s[3] = rotl(r.s[3], 45);
+    return result;
+}
+/* rand 0.8 UniformFloat<f64>: 52 random mantissa bits in [1,2), minus 1, * scale + low */
+double uniform(Rng &r, double low, double high) {
+    double scale = high - low;
+    const double max_rand = 1.0 - F64_EPS; /* largest value0_1 = 1 - 2^-52 */
+    while (scale * max_rand + low >= high) scale = std::nextafter(scale, 0.0);
+    const uint64_t bits = (next_u64(r) >> 12) | 0x3FF0000000000000ULL;
+    double value1_2;
+    std::memcpy(&value1_2, &bits, sizeof(double));
+    const double value0_1 = value1_2 - 1.0;
+    return value0_1 * scale + low;
+}
+double standard_normal(Rng &r) {
+    if (r.has_spare) {
+        r.has_spare = false;
+        return r.spare;
+    }
+    /* Box-Muller: u1 in (0,1], u2 in [0,1) */
+    const double u1 = 1.0 - uniform(r, 0.0, 1.0);
+    const double u2 = uniform(r, 0.0, 1.0);
+    const double rad = std::sqrt(-2.0 * std::log(u1));
+    const double ang = 2.0 * M_PI * u2;
+    r.spare = rad * std::sin(ang);
+    r.has_spare = true;
+    return rad * std::cos(ang);
+}
+
+/* random_su3 / rand_su3_with_dis, src/su3.rs:322-355 */
+V3 random_vec_3(Rng &r) {
+    V3 v;
+    for (int i = 0; i < 3; ++i) {
+        const double re = uniform(r, -1.0, 1.0);
+        const double im = uniform(r, -1.0, 1.0);
+        v.v[i] = cx(re, im);
+    }
+    return v;
+}
+M3 random_su3(Rng &r) {
+    V3 v1 = random_vec_3(r);
+    while (norm(v1) <= F64_EPS) v1 = random_vec_3(r);
+    V3 v2 = random_vec_3(r);
+    while (modulus(dot(v1, v2)) <= F64_EPS) v2 = random_vec_3(r);
+    return ortho_matrix_from_2_vector(v1, v2);
+}
+
+/* ---- lattice geometry, src/lattice.rs ---- */
+struct Lattice {
+    int D;
+    long L;
+    long V;
+    long pw[5];
+    Lattice(int d, long l) : D(d), L(l) {
+        pw[0] = 1;
+        for (int i = 1; i <= 4; ++i) pw[i] = pw[i - 1] * (i <= d ? l : 1);
+        V = pw[d];
+    }
+    /* LatticePoint::to_index, src/lattice.rs:909-916 */
+    long index(const long *x) const {
+        long s = 0;
+        for (int i = 0; i < D; ++i) s += (x[i] % L) * pw[i];
+        return s;
+    }
+    void coords(long site, long *x) const {
+        for (int i = 0; i < D; ++i) x[i] = (site / pw[i]) % L;
+    }
+    /* add_point_direction_n with n = 1, src/lattice.rs:303-323 */
+    long neighbour(long site, int mu, bool positive) const {
+        long x[4];
+        coords(site, x);
+        if (positive) {
+            x[mu] = (x[mu] + 1) % L;
+        } else {
+            if (x[mu] < 1) x[mu] = L - (1 - x[mu]);
+            else x[mu] = (x[mu] - 1) % L;
+        }
+        return index(x);
+    }
+};
+
+/* a signed direction: index + sign */
+struct Dir {
+    int index;
+    bool positive;
+};
+
+/* LinkMatrix::matrix, src/field.rs:726-740: U_{-mu}(x) = U_mu(x - mu)^dagger */
+inline M3 link_matrix(const Lattice &lat, const double *links, long site, Dir d) {
+    if (d.positive) return load_m3(links + (site * lat.D + d.index) * 18);
+    const long s = lat.neighbour(site, d.index, false);
+    return adjoint(load_m3(links + (s * lat.D + d.index) * 18));
+}
+inline long add_dir(const Lattice &lat, long site, Dir d) { return lat.neighbour(site, d.index, d.positive); }
+
+/* sij, src/field.rs:743-758: S_ij(x) = U_j(x) U_i(x+j) U_j(x+i)^dagger */
+inline M3 sij(const Lattice &lat, const double *links, long site, Dir di, Dir dj) {
+    const M3 u_j = link_matrix(lat, links, site, dj);
+    const long p_j = add_dir(lat, site, dj);
+    const M3 u_i_p_j = link_matrix(lat, links, p_j, di);
+    const long p_i = add_dir(lat, site, di);
+    const M3 u_j_pi_d = adjoint(link_matrix(lat, links, p_i, dj));
+    return (u_j * u_i_p_j) * u_j_pi_d;
+}
+/* pij, src/field.rs:761-771: P_ij(x) = U_i(x) S_ij(x)^dagger */
+inline M3 pij(const Lattice &lat, const double *links, long site, Dir di, Dir dj) {
+    const M3 s = sij(lat, links, site, di, dj);
+    const M3 u_i = link_matrix(lat, links, site, di);
+    return u_i * adjoint(s);
+}
+
+/* Direction::directions(): [+0, -0, +1, -1, ...], procedural_macro/src/lib.rs:53-83 */
+inline Dir direction_at(int k) { return Dir{k / 2, (k % 2) == 0}; }
+
+/* derivative_e at one site, src/simulation/state.rs:1420-1448 */
+void derivative_e_site(const Lattice &lat, const double *links, double size, long site, double *out /*D*8*/) {
+    const Generators &G = gens();
+    const double c = -std::sqrt(2.0 / 3.0);
+    for (int mu = 0; mu < lat.D; ++mu) {
+        const Dir dir{mu, true};
+        const M3 u_i = link_matrix(lat, links, site, dir);
+        M3 sum_s = zero3();
+        for (int k = 0; k < 2 * lat.D; ++k) {
+            const Dir d2 = direction_at(k);
+            if (d2.index == mu) continue;
+            sum_s = sum_s + adjoint(sij(lat, links, site, dir, d2));
+        }
+        for (int a = 0; a < 8; ++a) out[mu * 8 + a] = c * trace((G.g[a] * u_i) * sum_s).im / size;
+    }
+}
+
+/* derivative_u for one link, src/simulation/state.rs:1407-1417 */
+inline M3 derivative_u_link(const Lattice &lat, const double *links, const double *efield, double size, long site,
+                            int mu) {
+    const Cx c = cx(0.0, std::sqrt(2.0 * 3.0));
+    const M3 u_i = link_matrix(lat, links, site, Dir{mu, true});
+    const M3 e_i = to_matrix(efield + (site * lat.D + mu) * 8);
+    return ((e_i * u_i) * c) * cx(1.0 / size);
+}
+
+/* EField::gauss, src/field.rs:1174-1195 */
+M3 gauss_site(const Lattice &lat, const double *links, const double *efield, long site) {
+    M3 sum = zero3();
+    for (int mu = 0; mu < lat.D; ++mu) {
+        const M3 e_i = to_matrix(efield + (site * lat.D + mu) * 8);
+        const M3 u_mi = link_matrix(lat, links, site, Dir{mu, false});
+        const long p_mi = lat.neighbour(site, mu, false);
+        const M3 e_m_i = to_matrix(efield + (p_mi * lat.D + mu) * 8);
+        sum = sum + (e_i - (u_mi * e_m_i) * adjoint(u_mi));
+    }
+    return sum;
+}
+
+/* EField::gauss_sum_div, src/field.rs:1199-1220 */
+double gauss_sum_div(const Lattice &lat, const double *links, const double *efield) {
+    const M3 gsum = gens().sum;
+    double total = 0.0;
+#pragma omp parallel for reduction(+ : total) schedule(static)
+    for (long site = 0; site < lat.V; ++site) {
+        const M3 g = gauss_site(lat, links, efield, site);
+        total += modulus(trace(gsum * g));
+    }
+    return total;
+}
+
+/* EField::project_to_gauss_step, src/field.rs:1301-1337 */
+void project_to_gauss_step(const Lattice &lat, const double *links, const double *e_in, double *e_out) {
+    const Generators &G = gens();
+    const Cx K = cx(0.12, 0.0);
+#pragma omp parallel for schedule(static)
+    for (long site = 0; site < lat.V; ++site) {
+        for (int mu = 0; mu < lat.D; ++mu) {
+            const M3 u = link_matrix(lat, links, site, Dir{mu, true});
+            const M3 gauss = gauss_site(lat, links, e_in, site);
+            const M3 gauss_p = gauss_site(lat, links, e_in, lat.neighbour(site, mu, true));
+            const M3 inner = ((((u * gauss) * adjoint(u)) * gauss_p) - gauss) * K;
+            const double *e = e_in + (site * lat.D + mu) * 8;
+            for (int a = 0; a < 8; ++a) {
+                const M3 term = inner + G.g[a] * cx(e[a]);
+                e_out[(site * lat.D + mu) * 8 + a] = 2.0 * trace(G.g[a] * term).re;
+            }
+        }
+    }
+}
+
+/* EField::project_to_gauss, src/field.rs:1265-1294.  max_steps caps the loop (the
+ * reference has no cap); steps counts project_to_gauss_step calls (1 + 4k). */
+int project_to_gauss(const Lattice &lat, const double *links, const double *e_in, std::vector<double> &out,
+                     int max_steps, int *steps) {
+    const size_t n = (size_t)lat.V * lat.D * 8;
+    std::vector<double> cur(n), nxt(n);
+    project_to_gauss_step(lat, links, e_in, cur.data());
+    int done = 1;
+    const double threshold = F64_EPS * (double)(lat.V * 4 * 8 * 10);
+    for (;;) {
+        const double val_dif = gauss_sum_div(lat, links, cur.data());
+        if (std::isnan(val_dif)) {
+            if (steps) *steps = done;
+            return OR_ERR_GAUSS_PROJECTION;
+        }
+        if (val_dif <= threshold) break;
+        if (max_steps > 0 && done + 4 > max_steps) {
+            if (steps) *steps = done;
+            return OR_ERR_NOT_CONVERGED;
+        }
+        for (int k = 0; k < 4; ++k) {
+            project_to_gauss_step(lat, links, cur.data(), nxt.data());
+            cur.swap(nxt);
+            ++done;
+        }
+    }
+    out.swap(cur);
+    if (steps) *steps = done;
+    return OR_OK;
+}
+
+/* hamiltonian_links, src/simulation/state.rs:821-849 */
+double hamiltonian_links(const Lattice &lat, const double *links, double beta) {
+    double total = 0.0;
+#pragma omp parallel for reduction(+ : total) schedule(static)
+    for (long site = 0; site < lat.V; ++site) {
+        double s_site = 0.0;
+        for (int i = 0; i < lat.D; ++i) {
+            double s_i = 0.0;
+            for (int j = i + 1; j < lat.D; ++j) {
+                const M3 p = pij(lat, links, site, Dir{i, true}, Dir{j, true});
+                s_i = s_i + (1.0 - trace(p).re / 3.0);
+            }
+            s_site = s_site + s_i;
+        }
+        total += s_site;
+    }
+    return total * beta;
+}
+
+/* hamiltonian_efield, src/simulation/state.rs:1370-1385 */
+double hamiltonian_efield(const Lattice &lat, const double *efield, double beta) {
+    double total = 0.0;
+#pragma omp parallel for reduction(+ : total) schedule(static)
+    for (long site = 0; site < lat.V; ++site) {
+        double s = 0.0;
+        for (int mu = 0; mu < lat.D; ++mu) s = s + trace_squared(efield + (site * lat.D + mu) * 8);
+        total += s;
+    }
+    return total * beta;
+}
+
+/* SymplecticEulerRayon::link_matrix_integrate + integrate_link,
+ * src/integrator/symplectic_euler_rayon.rs:65-81, src/integrator/mod.rs:216-233.
+ * A new buffer per call, as in the reference. */
+std::vector<double> link_matrix_integrate(const Lattice &lat, const double *links, const double *efield, double size,
+                                          double dt) {
+    std::vector<double> out((size_t)lat.V * lat.D * 18);
+#pragma omp parallel for schedule(static)
+    for (long site = 0; site < lat.V; ++site) {
+        for (int mu = 0; mu < lat.D; ++mu) {
+            const M3 init = load_m3(links + (site * lat.D + mu) * 18);
+            const M3 du = derivative_u_link(lat, links, efield, size, site, mu);
+            store_m3(init + du * cx(dt), out.data() + (site * lat.D + mu) * 18);
+        }
+    }
+    return out;
+}
+
+/* SymplecticEulerRayon::e_field_integrate + integrate_efield,
+ * src/integrator/symplectic_euler_rayon.rs:88-104, src/integrator/mod.rs:240-254 */
+std::vector<double> e_field_integrate(const Lattice &lat, const double *links, const double *efield, double size,
+                                      double dt) {
+    std::vector<double> out((size_t)lat.V * lat.D * 8);
+#pragma omp parallel for schedule(static)
+    for (long site = 0; site < lat.V; ++site) {
+        double deriv[4 * 8];
+        derivative_e_site(lat, links, size, site, deriv);
+        for (int mu = 0; mu < lat.D; ++mu)
+            for (int a = 0; a < 8; ++a) {
+                const size_t k = ((size_t)site * lat.D + mu) * 8 + a;
+                out[k] = efield[k] + deriv[mu * 8 + a] * dt;
+            }
+    }
+    return out;
+}
+
+struct Fields {
+    std::vector<double> links, efield;
+};
+
+/* SymplecticIntegrator for SymplecticEulerRayon, src/integrator/symplectic_euler_rayon.rs:120-252 */
+Fields integrate_once(const Lattice &lat, const Fields &in, double size, int mode, double dt) {
+    Fields out;
+    switch (mode) {
+    case OR_SYNC_SYNC:
+        out.links = link_matrix_integrate(lat, in.links.data(), in.efield.data(), size, dt);
+        out.efield = e_field_integrate(lat, in.links.data(), in.efield.data(), size, dt);
+        break;
+    case OR_LEAP_LEAP:
+        out.links = link_matrix_integrate(lat, in.links.data(), in.efield.data(), size, dt);
+        out.efield = e_field_integrate(lat, out.links.data(), in.efield.data(), size, dt);
+        break;
+    case OR_SYNC_LEAP:
+        out.efield = e_field_integrate(lat, in.links.data(), in.efield.data(), size, dt / 2.0);
+        out.links = in.links;
+        break;
+    case OR_LEAP_SYNC:
+        out.links = link_matrix_integrate(lat, in.links.data(), in.efield.data(), size, dt);
+        out.efield = e_field_integrate(lat, out.links.data(), in.efield.data(), size, dt / 2.0);
+        break;
+    default: { /* OR_SYMPLECTIC */
+        const std::vector<double> e_half = e_field_integrate(lat, in.links.data(), in.efield.data(), size, dt / 2.0);
+        out.links = link_matrix_integrate(lat, in.links.data(), e_half.data(), size, dt);
+        out.efield = e_field_integrate(lat, out.links.data(), e_half.data(), size, dt / 2.0);
+        break;
+    }
+    }
+    return out;
+}
+
+bool supported_dim(int dim) { return dim >= 2 && dim <= 4; }
+
+int check_lattice(int dim, long L) {
+    if (dim == 0) return OR_ERR_ZERO_DIMENSION;
+    if (!supported_dim(dim)) return OR_ERR_UNSUPPORTED_D;
+    if (L < 2) return OR_ERR_DIM_TOO_SMALL;
+    return OR_OK;
+}
+
+} // namespace
+
+/* ======================= C interface ======================= */
+
+extern "C" {
+
+void *or_rng_new(uint64_t seed) {
+    Rng *r = new Rng();
+    uint64_t x = seed;
+    for (int i = 0; i < 4; ++i) r->s[i] = splitmix64(x);
+    return r;
+}
+void or_rng_free(void *rng) { delete static_cast<Rng *>(rng); }
+uint64_t or_rng_next_u64(void *rng) { return next_u64(*static_cast<Rng *>(rng)); }
+double or_rng_uniform(void *rng, double low, double high) { return uniform(*static_cast<Rng *>(rng), low, high); }
+double or_rng_standard_normal(void *rng) { return standard_normal(*static_cast<Rng *>(rng)); }
+
+/* LatticeCyclic::new, src/lattice.rs:190-201 (checks in the same order) */
+int or_lattice_new(int dim, double size, long number_of_points) {
+    if (dim == 0) return OR_ERR_ZERO_DIMENSION;
+    if (size <= 0.0 || std::isnan(size) || std::isinf(size)) return OR_ERR_NON_POSITIVE_SIZE;
+    if (number_of_points < 2) return OR_ERR_DIM_TOO_SMALL;
+    if (!supported_dim(dim)) return OR_ERR_UNSUPPORTED_D;
+    return OR_OK;
+}
+
+void or_generators(double *out) {
+    for (int a = 0; a < 8; ++a) store_m3(gens().g[a], out + 18 * a);
+}
+void or_su3_to_matrix(const double *adj8, double *out18) { store_m3(to_matrix(adj8), out18); }
+void or_su3_exp_i(const double *adj8, double *out18) { store_m3(su3_exp_i(adj8), out18); }
+void or_su3_exp_r(const double *adj8, double *out18) { store_m3(su3_exp_r(adj8), out18); }
+void or_orthonormalize(const double *m18, double *out18) { store_m3(orthonormalize_matrix(load_m3(m18)), out18); }
+void or_random_su3(void *rng, double *out18) { store_m3(random_su3(*static_cast<Rng *>(rng)), out18); }
+void or_matmul(const double *a18, const double *b18, double *out18) { store_m3(load_m3(a18) * load_m3(b18), out18); }
+void or_determinant(const double *m18, double *out2) {
+    const Cx d = determinant(load_m3(m18));
+    out2[0] = d.re;
+    out2[1] = d.im;
+}
+
+/* LinkMatrix::new_determinist, src/field.rs:646-659: one random_su3 per link, link order */
+int or_links_random(int dim, int L, void *rng, double *links) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    Rng &r = *static_cast<Rng *>(rng);
+    for (long k = 0; k < lat.V * dim; ++k) store_m3(random_su3(r), links + k * 18);
+    return OR_OK;
+}
+/* LinkMatrix::new_cold, src/field.rs:703-707 */
+int or_links_cold(int dim, int L, double *links) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    for (long k = 0; k < lat.V * dim; ++k) store_m3(identity3(), links + k * 18);
+    return OR_OK;
+}
+/* EField::new_determinist, src/field.rs:1086-1099: site order, then mu, then a */
+int or_efield_normal(int dim, int L, void *rng, double std_dev, double *efield) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    if (!(std_dev >= 0.0) || std::isinf(std_dev)) return OR_ERR_INVALID_NORMAL;
+    const Lattice lat(dim, L);
+    Rng &r = *static_cast<Rng *>(rng);
+    for (long k = 0; k < lat.V * dim * 8; ++k) efield[k] = 0.0 + std_dev * standard_normal(r);
+    return OR_OK;
+}
+
+int or_hamiltonian_links(int dim, int L, double beta, const double *links, double *out) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    *out = hamiltonian_links(Lattice(dim, L), links, beta);
+    return OR_OK;
+}
+int or_hamiltonian_efield(int dim, int L, double beta, const double *efield, double *out) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    *out = hamiltonian_efield(Lattice(dim, L), efield, beta);
+    return OR_OK;
+}
+/* LinkMatrix::average_trace_plaquette, src/field.rs:775-804 */
+int or_average_trace_plaquette(int dim, int L, const double *links, double *re, double *im) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    double sre = 0.0, sim = 0.0;
+#pragma omp parallel for reduction(+ : sre, sim) schedule(static)
+    for (long site = 0; site < lat.V; ++site) {
+        Cx s_site = cx(0.0);
+        for (int i = 0; i < dim; ++i) {
+            Cx s_i = cx(0.0);
+            for (int j = i + 1; j < dim; ++j) s_i = s_i + trace(pij(lat, links, site, Dir{i, true}, Dir{j, true}));
+            s_site = s_site + s_i;
+        }
+        sre += s_site.re;
+        sim += s_site.im;
+    }
+    const double n_plaq = (double)(lat.V * ((dim * (dim - 1)) / 2));
+    *re = sre / n_plaq;
+    *im = sim / n_plaq;
+    return OR_OK;
+}
+int or_gauss(int dim, int L, const double *links, const double *efield, long site, double *out18) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    if (site < 0 || site >= lat.V) return OR_ERR_INVALID_ARGUMENT;
+    store_m3(gauss_site(lat, links, efield, site), out18);
+    return OR_OK;
+}
+int or_gauss_sum_div(int dim, int L, const double *links, const double *efield, double *out) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    *out = gauss_sum_div(Lattice(dim, L), links, efield);
+    return OR_OK;
+}
+int or_project_to_gauss(int dim, int L, const double *links, const double *efield_in, double *efield_out,
+                        int max_steps, int *steps_done) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    std::vector<double> out;
+    const int rc = project_to_gauss(lat, links, efield_in, out, max_steps, steps_done);
+    if (rc) return rc;
+    std::memcpy(efield_out, out.data(), out.size() * sizeof(double));
+    return OR_OK;
+}
+/* LinkMatrix::normalize, src/field.rs:897-901 */
+int or_normalize(int dim, int L, double *links) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < lat.V * dim; ++k) store_m3(orthonormalize_matrix(load_m3(links + k * 18)), links + k * 18);
+    return OR_OK;
+}
+int or_derivative_e(int dim, int L, double size, const double *links, double *force) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+#pragma omp parallel for schedule(static)
+    for (long site = 0; site < lat.V; ++site) derivative_e_site(lat, links, size, site, force + site * dim * 8);
+    return OR_OK;
+}
+int or_derivative_u(int dim, int L, double size, const double *links, const double *efield, double *du) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+#pragma omp parallel for schedule(static)
+    for (long site = 0; site < lat.V; ++site)
+        for (int mu = 0; mu < dim; ++mu)
+            store_m3(derivative_u_link(lat, links, efield, size, site, mu), du + (site * dim + mu) * 18);
+    return OR_OK;
+}
+
+/* simulate_{sync,leap,symplectic}_n, src/simulation/state.rs:399-491 and :603-647 */
+int or_integrate(int dim, int L, double size, const double *links_in, const double *efield_in, int mode, double dt,
+                 int n, double *links_out, double *efield_out) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    if (n <= 0) return OR_ERR_ZERO_INTEGRATION;
+    if (mode < OR_SYNC_SYNC || mode > OR_SYMPLECTIC) return OR_ERR_INVALID_ARGUMENT;
+    const Lattice lat(dim, L);
+    Fields f;
+    f.links.assign(links_in, links_in + (size_t)lat.V * dim * 18);
+    f.efield.assign(efield_in, efield_in + (size_t)lat.V * dim * 8);
+    for (int i = 0; i < n; ++i) f = integrate_once(lat, f, size, mode, dt);
+    std::memcpy(links_out, f.links.data(), f.links.size() * sizeof(double));
+    std::memcpy(efield_out, f.efield.data(), f.efield.size() * sizeof(double));
+    return OR_OK;
+}
+
+/* simulate_using_leapfrog_n, src/simulation/state.rs:318-357 */
+int or_leapfrog_n(int dim, int L, double size, const double *links_in, const double *efield_in, double dt, int n,
+                  double *links_out, double *efield_out) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    if (n <= 0) return OR_ERR_ZERO_INTEGRATION;
+    const Lattice lat(dim, L);
+    Fields f;
+    f.links.assign(links_in, links_in + (size_t)lat.V * dim * 18);
+    f.efield.assign(efield_in, efield_in + (size_t)lat.V * dim * 8);
+    f = integrate_once(lat, f, size, OR_SYNC_LEAP, dt);
+    for (int i = 1; i < n; ++i) f = integrate_once(lat, f, size, OR_LEAP_LEAP, dt);
+    f = integrate_once(lat, f, size, OR_LEAP_SYNC, dt);
+    std::memcpy(links_out, f.links.data(), f.links.size() * sizeof(double));
+    std::memcpy(efield_out, f.efield.data(), f.efield.size() * sizeof(double));
+    return OR_OK;
+}
+
+/* HybridMonteCarloDiagnostic::next_element with injected randomness,
+ * src/simulation/monte_carlo/hybrid_monte_carlo.rs:465-471 and :573-613 */
+int or_hmc_trajectory(int dim, int L, double size, double beta, const double *links_in, const double *efield_raw,
+                      double dt, int n_steps, double uniform_draw, int max_gauss_steps, double *links_out,
+                      double *efield_out, int *accepted, double *prob, double *h_old, double *h_new,
+                      int *gauss_steps) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const double std_dev = 0.5 / beta; /* Normal(0, 0.5/beta) must be a valid distribution */
+    if (!(std_dev >= 0.0) || std::isinf(std_dev)) return OR_ERR_INVALID_NORMAL;
+    if (n_steps <= 0) return OR_ERR_ZERO_INTEGRATION;
+    const Lattice lat(dim, L);
+    /* new_random_e_state: project the drawn field, src/simulation/state.rs:1093-1108 */
+    std::vector<double> e_proj;
+    const int rc = project_to_gauss(lat, links_in, efield_raw, e_proj, max_gauss_steps, gauss_steps);
+    if (rc) return rc;
+    Fields f0;
+    f0.links.assign(links_in, links_in + (size_t)lat.V * dim * 18);
+    f0.efield = e_proj;
+    Fields f = f0;
+    for (int i = 0; i < n_steps; ++i) f = integrate_once(lat, f, size, OR_SYMPLECTIC, dt);
+    /* probability_of_replacement, hybrid_monte_carlo.rs:584-589 */
+    const double h0 = hamiltonian_links(lat, f0.links.data(), beta) + hamiltonian_efield(lat, f0.efield.data(), beta);
+    const double h1 = hamiltonian_links(lat, f.links.data(), beta) + hamiltonian_efield(lat, f.efield.data(), beta);
+    double p = std::fmax(std::fmin(std::exp(h0 - h1), 1.0), 0.0);
+    p = std::fmax(std::fmin(p, 1.0), 0.0);
+    /* rand 0.8 Bernoulli: p == 1 is always true, otherwise u < p */
+    const bool acc = (p >= 1.0) || (uniform_draw < p);
+    const Fields &res = acc ? f : f0;
+    std::memcpy(links_out, res.links.data(), res.links.size() * sizeof(double));
+    if (efield_out) std::memcpy(efield_out, res.efield.data(), res.efield.size() * sizeof(double));
+    *accepted = acc ? 1 : 0;
+    *prob = p;
+    *h_old = h0;
+    *h_new = h1;
+    return OR_OK;
+}
+
+void or_set_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+}
+int or_get_threads(void) { return omp_get_max_threads(); }
+
+} /* extern "C" */

@@ -1,0 +1,78 @@
+"""C ABI surface checks that need no GPU: the library builds and loads, every entry point
+declared in include/lqgpu.h is exported and bound, and without a device the library
+fails loudly instead of falling back to the CPU."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import REPO
+
+HEADER = os.path.join(REPO, "include", "lqgpu.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(lq_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("lq_state_create", "lq_integrate", "lq_hmc_trajectory", "lq_project_gauss",
+                     "lq_hamiltonian_links", "lq_average_trace_plaquette", "lq_normalize_link_matrices"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(lqgpu_mod):
+    lib = lqgpu_mod.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    # and the binding knows every one of them (signatures are set, none forgotten)
+    assert set(declared_functions()) == set(lqgpu_mod.SIGNATURES)
+
+
+def test_dynamic_symbol_table(lqgpu_mod):
+    out = subprocess.run(["nm", "-D", "--defined-only", lqgpu_mod.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (lq_[a-z0-9_]+)\b", out))
+    assert set(declared_functions()) <= exported
+
+
+def test_status_strings(lqgpu_mod):
+    lib = lqgpu_mod.load()
+    assert lib.lq_status_string(0) == b"ok"
+    assert b"dimension" in lib.lq_status_string(lqgpu_mod.LQ_ERR_UNSUPPORTED_DIM)
+    assert lib.lq_version() >= 100
+
+
+def test_argument_validation_precedes_device_use(lqgpu_mod):
+    """LatticeCyclic::new validation order (src/lattice.rs:190-201) is checked on the host
+    before any device call."""
+    lib = lqgpu_mod.load()
+    h = ctypes.c_void_p()
+    assert lib.lq_state_create(0, 4, 1.0, 1.0, 0, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_ZERO_DIMENSION
+    assert lib.lq_state_create(4, 4, 0.0, 1.0, 0, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_NON_POSITIVE_SIZE
+    assert lib.lq_state_create(4, 4, float("nan"), 1.0, 0, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_NON_POSITIVE_SIZE
+    assert lib.lq_state_create(4, 4, float("inf"), 1.0, 0, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_NON_POSITIVE_SIZE
+    assert lib.lq_state_create(3, 1, 1.0, 1.0, 0, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_DIM_TOO_SMALL
+    assert lib.lq_state_create(5, 4, 1.0, 1.0, 0, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_UNSUPPORTED_DIM
+    assert lib.lq_state_create(1, 4, 1.0, 1.0, 0, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_UNSUPPORTED_DIM
+    assert lib.lq_state_create(4, 4, 1.0, 1.0, 7, ctypes.byref(h)) == lqgpu_mod.LQ_ERR_INVALID_ARGUMENT
+    assert lib.lq_state_create(4, 4, 1.0, 1.0, 0, None) == lqgpu_mod.LQ_ERR_INVALID_ARGUMENT
+    # null handles are rejected, never dereferenced
+    assert lib.lq_integrate(None, 4, 0.1, 1) == lqgpu_mod.LQ_ERR_INVALID_ARGUMENT
+    assert lib.lq_hmc_decide(None, 1) == lqgpu_mod.LQ_ERR_INVALID_ARGUMENT
+
+
+def test_no_cpu_fallback_without_device(lqgpu_mod):
+    lib = lqgpu_mod.load()
+    h = ctypes.c_void_p()
+    rc = lib.lq_state_create(2, 4, 1.0, 1.0, 0, ctypes.byref(h))
+    if rc == lqgpu_mod.LQ_OK:
+        lib.lq_state_destroy(h)
+        pytest.skip("a CUDA device is visible; the no-device path is not reachable here")
+    assert rc == lqgpu_mod.LQ_ERR_NO_DEVICE
+    with pytest.raises(lqgpu_mod.LqError):
+        lqgpu_mod.State(2, 4)

@@ -4,7 +4,7 @@
 // Device layout (structure of arrays, one plane per matrix/vector component):
 //   links  U : vec2<T>[D][9][V]   U[(mu*9 + k)*V + site], k = row*3 + col
 //   efield E : T[D][8][V]          E[(mu*8 + a)*V + site]
-//   gauss  G : T[8][V]             g^a(x) = 2 Re Tr(T^a G(x))
+//   gauss  G : T[9][V]             Hermitian G(x): real diagonal + upper off-diagonal
 // Sites are linearised x_0 fastest as in the reference (src/lattice.rs:909-916), so the
 // +-mu neighbour of a site is +-L^mu with periodic wrap, and consecutive threads touch
 // consecutive addresses of every plane (coalesced 128-bit/64-bit accesses).
@@ -170,10 +170,44 @@ __global__ void __launch_bounds__(128) k_md(const V2<T> *__restrict__ Uin, V2<T>
 }
 
 // ------------------------------------------------------------------ Gauss law
+// G(x) is Hermitian; it is stored as 9 reals per site: the real diagonal and the upper
+// off-diagonal entries, G[c*V + site] with c = (G00, G11, G22, Re G01, Im G01, Re G02,
+// Im G02, Re G12, Im G12).  Links drift off SU(3) under the first-order link update, so
+// U^dag E U acquires a small trace; keeping the full Hermitian G (not only its su(3)
+// projection) follows the reference, whose G enters the projection step as a matrix.
+template <typename T> __device__ __forceinline__ void herm_load(const T *__restrict__ G, size_t V, uint32_t site,
+                                                                mat3<T> &m) {
+    const T d0 = G[site], d1 = G[V + site], d2 = G[2 * V + site];
+    const T r01 = G[3 * V + site], i01 = G[4 * V + site];
+    const T r02 = G[5 * V + site], i02 = G[6 * V + site];
+    const T r12 = G[7 * V + site], i12 = G[8 * V + site];
+    m.e[0] = cmk(d0, T(0));
+    m.e[4] = cmk(d1, T(0));
+    m.e[8] = cmk(d2, T(0));
+    m.e[1] = cmk(r01, i01);
+    m.e[3] = cmk(r01, -i01);
+    m.e[2] = cmk(r02, i02);
+    m.e[6] = cmk(r02, -i02);
+    m.e[5] = cmk(r12, i12);
+    m.e[7] = cmk(r12, -i12);
+}
+template <typename T> __device__ __forceinline__ void herm_store(T *__restrict__ G, size_t V, uint32_t site,
+                                                                 const mat3<T> &m) {
+    G[site] = m.e[0].re;
+    G[V + site] = m.e[4].re;
+    G[2 * V + site] = m.e[8].re;
+    G[3 * V + site] = m.e[1].re;
+    G[4 * V + site] = m.e[1].im;
+    G[5 * V + site] = m.e[2].re;
+    G[6 * V + site] = m.e[2].im;
+    G[7 * V + site] = m.e[5].re;
+    G[8 * V + site] = m.e[5].im;
+}
+
 // G(x) = sum_mu [E_mu(x) - U_mu(x-mu)^dag E_mu(x-mu) U_mu(x-mu)]  (EField::gauss,
-// src/field.rs:1174-1195), stored as 8 coefficients; the per-site residual
-// |Tr((sum_a T^a) G(x))| = |sum_a g^a| / 2 (gauss_sum_div, src/field.rs:1199-1220) is
-// reduced into one partial per block.
+// src/field.rs:1174-1195); the per-site residual |Tr((sum_a T^a) G(x))| = |sum_a g^a| / 2,
+// g^a = 2 Re Tr(T^a G) (gauss_sum_div, src/field.rs:1199-1220), is reduced into one
+// partial per block.
 template <int D, typename T>
 __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, const T *__restrict__ E,
                                                T *__restrict__ G, Geo<D> g, double *__restrict__ partial) {
@@ -183,34 +217,35 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
         const size_t V = g.V;
         uint32_t c[D];
         site_coords(g, site, c);
-        T gs[8];
-#pragma unroll
-        for (int a = 0; a < 8; ++a) gs[a] = T(0);
+        mat3<T> gs;
+        mat_zero(gs);
 #pragma unroll
         for (int mu = 0; mu < D; ++mu) {
             const uint32_t xm = bwd(g, site, c[mu], mu);
-            T em_c[8];
+            T ex_c[8], em_c[8];
 #pragma unroll
             for (int a = 0; a < 8; ++a) {
-                gs[a] += E[(size_t)(mu * 8 + a) * V + site];
+                ex_c[a] = E[(size_t)(mu * 8 + a) * V + site];
                 em_c[a] = E[(size_t)(mu * 8 + a) * V + xm];
             }
-            mat3<T> u, em, t, w;
+            mat3<T> u, ex, em, t, w;
             load_link<T>(U, (size_t)(mu * 9) * V, V, xm, u);
+            adjoint_to_matrix<T>(ex_c, ex);
             adjoint_to_matrix<T>(em_c, em);
             mul_nn(em, u, t);
             mul_an(u, t, w);
-            T wc[8];
-            two_re_tr_generators(w, wc);
 #pragma unroll
-            for (int a = 0; a < 8; ++a) gs[a] -= wc[a];
+            for (int k = 0; k < 9; ++k) {
+                gs.e[k].re += ex.e[k].re - w.e[k].re;
+                gs.e[k].im += ex.e[k].im - w.e[k].im;
+            }
         }
+        herm_store(G, V, site, gs);
+        T gc[8];
+        two_re_tr_generators(gs, gc);
         double s = 0.0;
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            G[(size_t)a * V + site] = gs[a];
-            s += (double)gs[a];
-        }
+        for (int a = 0; a < 8; ++a) s += (double)gc[a];
         r[0] = fabs(s) * 0.5;
     }
     block_reduce_store<1>(r, partial, blockIdx.x, gridDim.x);
@@ -218,7 +253,7 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
 
 // One projection step on link (x, mu) (EField::project_to_gauss_step, src/field.rs:1301-1337):
 //   e'^a = 2 Re Tr(T^a [(u G(x) u^dag G(x+mu) - G(x)) K + T^a e^a]),  K = 0.12
-//        = e^a + K (2 Re Tr(T^a u G(x) u^dag G(x+mu)) - g^a(x))
+//        = e^a + K (2 Re Tr(T^a u G(x) u^dag G(x+mu)) - 2 Re Tr(T^a G(x)))
 // E is updated in place: each thread reads and writes only its own link.
 template <int D, typename T>
 __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U, T *__restrict__ E,
@@ -230,26 +265,21 @@ __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U,
     uint32_t c[D];
     site_coords(g, site, c);
     const uint32_t xp = fwd(g, site, c[mu], mu);
-    T gx[8], gp[8];
-#pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        gx[a] = G[(size_t)a * V + site];
-        gp[a] = G[(size_t)a * V + xp];
-    }
     mat3<T> u, gm, gpm, t1, t2, x;
+    herm_load(G, V, site, gm);
+    herm_load(G, V, xp, gpm);
     load_link<T>(U, (size_t)(mu * 9) * V, V, site, u);
-    adjoint_to_matrix<T>(gx, gm);
-    adjoint_to_matrix<T>(gp, gpm);
     mul_nn(u, gm, t1);
     mul_na(t1, u, t2);
     mul_nn(t2, gpm, x);
-    T xc[8];
+    T xc[8], gc[8];
     two_re_tr_generators(x, xc);
+    two_re_tr_generators(gm, gc);
     const T K = T(0.12);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
         const size_t idx = (size_t)(mu * 8 + a) * V + site;
-        E[idx] = fma(K, xc[a] - gx[a], E[idx]);
+        E[idx] = fma(K, xc[a] - gc[a], E[idx]);
     }
 }
 
@@ -445,12 +475,17 @@ __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, 
 #pragma unroll
     for (int a = 0; a < 8; ++a) dst[a] = (double)E[(size_t)(mu * 8 + a) * V + site];
 }
+// G(x) as its 8 su(3) coefficients g^a = 2 Re Tr(T^a G(x))
 template <typename T>
 __global__ void __launch_bounds__(256) k_gauss_to_aos(const T *__restrict__ G, double *__restrict__ out, uint32_t V) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     if (site >= V) return;
+    mat3<T> m;
+    herm_load(G, (size_t)V, site, m);
+    T gc[8];
+    two_re_tr_generators(m, gc);
 #pragma unroll
-    for (int a = 0; a < 8; ++a) out[(size_t)site * 8 + a] = (double)G[(size_t)a * V + site];
+    for (int a = 0; a < 8; ++a) out[(size_t)site * 8 + a] = (double)gc[a];
 }
 
 template <typename T>

@@ -36,7 +36,7 @@ struct State {
     void *U[3] = {nullptr, nullptr, nullptr}; // link buffers (SoA); U[cur] is the state
     int cur = 0;
     void *E = nullptr;   // E-field (SoA)
-    void *G = nullptr;   // Gauss-law coefficients, 8 per site
+    void *G = nullptr;   // Gauss-law matrix G(x), Hermitian, 9 reals per site
     double *partial = nullptr;
     uint32_t partial_slots = 0; // slots per row of `partial`
     double *d_out = nullptr;    // device scalars
@@ -63,7 +63,7 @@ struct State {
     size_t link_bytes() const { return link_elems() * 2 * real_bytes; }
     size_t efield_elems() const { return (size_t)V * dim * 8; } // reals
     size_t efield_bytes() const { return efield_elems() * real_bytes; }
-    size_t gauss_bytes() const { return (size_t)V * 8 * real_bytes; }
+    size_t gauss_bytes() const { return (size_t)V * 9 * real_bytes; }
 };
 
 // Device operations of one (D, T) instantiation.  Launches are asynchronous on s.stream

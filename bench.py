@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--dt", type=float, default=0.005)
     ap.add_argument("--md-steps", type=int, default=20)
     ap.add_argument("--size", type=float, default=1000.0)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "f64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "f32", "f64"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed FP64 trajectories for the comparison leg")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample-L", type=int, default=8)
@@ -205,7 +205,9 @@ def run_reference(args):
 def algorithmic_md_bytes(n_links, md_steps, real_bytes):
     """Bytes moved by the fused MD kernels of one trajectory at ideal neighbour reuse.
     kick+drift launch: read U (18 reals) + E (8) + write E (8) + U' (18) = 52 reals per link;
-    final kick-only launch: read U (18) + E (8) + write E (8) = 34 reals per link."""
+    final kick-only launch: read U (18) + E (8) + write E (8) = 34 reals per link.
+    real_bytes is the stored size of one real: 8 for FP64 and for the compensated FP32 pairs
+    of the mixed form, 4 for plain FP32 storage."""
     return n_links * real_bytes * (52 * md_steps + 34)
 
 
@@ -232,8 +234,8 @@ def run_ours(args):
 
     dim, L, beta, dt, nmd, size = args.dim, args.L, args.beta, args.dt, args.md_steps, args.size
     n_links = L ** dim * dim
-    prec = lqgpu.PRECISION_MIXED if args.precision == "mixed" else lqgpu.PRECISION_F64
-    real_bytes = 4 if prec == lqgpu.PRECISION_MIXED else 8
+    prec = {"mixed": lqgpu.PRECISION_MIXED, "f32": lqgpu.PRECISION_F32, "f64": lqgpu.PRECISION_F64}[args.precision]
+    real_bytes = 4 if prec == lqgpu.PRECISION_F32 else 8
     uni = np.random.default_rng(1000 + rank)
 
     def barrier():
@@ -329,10 +331,11 @@ def run_ours(args):
     plaq_mixed = s.average_trace_plaquette()
     s.close()
 
-    # ---- FP64 leg (the plain GPU form) and accuracy at equal inputs
+    # ---- FP64 leg (the plain GPU form), the plain-FP32-storage leg, and accuracy at equal inputs
     fp64 = None
+    f32 = None
     accuracy = None
-    if prec == lqgpu.PRECISION_MIXED and args.fp64_steps > 0:
+    if prec != lqgpu.PRECISION_F64 and args.fp64_steps > 0:
         s64 = lqgpu.State(dim, L, size, beta, lqgpu.PRECISION_F64)
         s64.set_stream(stream.cuda_stream)
         s64.set_links_random(1 + rank)
@@ -342,32 +345,46 @@ def run_ours(args):
         v64 = sum_over_ranks(n_links * nmd * args.fp64_steps) / (ms64 / 1000.0)
         md64_n, md64_ms = prof64["md"]
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.fp64_steps,
-                "mixed_over_fp64": value / v64,
+                "headline_over_fp64": value / v64,
                 "md_kernel_ms": md64_ms / max(1, md64_n),
                 "gauss_steps": [r["gauss_steps"] for r in res64]}
+        other = lqgpu.PRECISION_F32 if prec == lqgpu.PRECISION_MIXED else lqgpu.PRECISION_MIXED
+        so = lqgpu.State(dim, L, size, beta, other)
+        so.set_stream(stream.cuda_stream)
+        so.set_links_random(1 + rank)
+        so.profile_enable(True)
+        mso, _, profo, reso, _ = timed_trajectories(so, 1, max(2, args.fp64_steps), 77 + rank)
+        mso = max_over_ranks(mso)
+        vo = sum_over_ranks(n_links * nmd * max(2, args.fp64_steps)) / (mso / 1000.0)
+        f32 = {"precision": "f32" if other == lqgpu.PRECISION_F32 else "mixed", "value": vo, "unit": UNIT,
+               "ms_per_step": mso / max(2, args.fp64_steps),
+               "md_kernel_ms": profo["md"][1] / max(1, profo["md"][0])}
         if not args.no_accuracy:
-            # identical momenta (host draw) and uniforms into both precisions, from identical links
+            # identical links, momenta (host draw) and uniforms into every precision
             sm = lqgpu.State(dim, L, size, beta, lqgpu.PRECISION_MIXED)
-            sm.set_links_random(5)
-            s64.set_links_random(5)
+            sf = lqgpu.State(dim, L, size, beta, lqgpu.PRECISION_F32)
+            states = {"f64": s64, "mixed": sm, "f32": sf}
+            for st in states.values():
+                st.set_links_random(5)
             rngacc = np.random.default_rng(9)
-            errs_dh, errs_pl, dhs = [], [], []
+            acc_out = {k: [] for k in states}
             for k in range(2):
                 e_raw = rngacc.normal(0.0, 0.5 / beta, size=(L ** dim, dim, 8))
                 u = float(rngacc.uniform())
-                out = []
-                for st in (s64, sm):
+                for name, st in states.items():
                     st.hmc_refresh_upload(e_raw)
                     p, h0, h1 = st.hmc_propose(dt, nmd)
                     st.hmc_decide(p >= 1.0 or u < p)
-                    out.append((h1 - h0, st.average_trace_plaquette().real / 3.0))
-                errs_dh.append(abs(out[0][0] - out[1][0]))
-                errs_pl.append(abs(out[0][1] - out[1][1]))
-                dhs.append(out[0][0])
-            accuracy = {"trajectories": 2, "max_abs_delta_h_error": max(errs_dh),
-                        "max_abs_plaquette_error": max(errs_pl), "fp64_delta_h": dhs,
-                        "note": "mixed vs FP64 GPU from identical links, momenta and uniforms"}
+                    acc_out[name].append((h1 - h0, st.average_trace_plaquette().real / 3.0))
+            accuracy = {"trajectories": 2, "fp64_delta_h": [x[0] for x in acc_out["f64"]],
+                        "note": "every precision vs FP64 GPU from identical links, momenta and uniforms"}
+            for name in ("mixed", "f32"):
+                accuracy[name] = {
+                    "max_abs_delta_h_error": max(abs(a[0] - b[0]) for a, b in zip(acc_out[name], acc_out["f64"])),
+                    "max_abs_plaquette_error": max(abs(a[1] - b[1]) for a, b in zip(acc_out[name], acc_out["f64"]))}
             sm.close()
+            sf.close()
+        so.close()
         s64.close()
 
     cpu = None
@@ -382,7 +399,9 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64" if prec == lqgpu.PRECISION_MIXED else "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": {lqgpu.PRECISION_MIXED: "f32 (compensated f32 pairs stored) + f64 sums",
+                                           lqgpu.PRECISION_F32: "f32 + f64 sums",
+                                           lqgpu.PRECISION_F64: "f64"}[prec], "data": "synthetic",
             "config": {"workload": "HMC trajectory D=%d %d^%d, beta %g, %d leap-frog steps dt %g, size %g, "
                                    "random_su3 start, device momenta N(0,0.5/beta) + Gauss projection"
                                    % (dim, L, dim, beta, nmd, dt, size),
@@ -396,7 +415,8 @@ def run_ours(args):
             "gpu_launches": launches,
             "gauss_steps": gauss_steps, "acceptance": acc_rate, "plaquette": plaq_mixed.real / 3.0,
             "wall_ms_per_step": 1000.0 * wall / args.steps,
-            "clocks": clocks, "e2e": e2e, "fp64": fp64, "accuracy": accuracy, "cpu_baseline": cpu,
+            "clocks": clocks, "e2e": e2e, "fp64": fp64, "other_precision": f32, "accuracy": accuracy,
+            "cpu_baseline": cpu,
         }
         print(json.dumps(line))
     if pg is not None:

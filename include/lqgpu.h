@@ -58,7 +58,12 @@ enum lq_status {
 /* arithmetic of the state */
 enum lq_precision {
     LQ_PRECISION_F64 = 0,   /* FP64 throughout: parity form */
-    LQ_PRECISION_MIXED = 1  /* FP32 links/E/force, FP64 reductions and reprojection */
+    LQ_PRECISION_MIXED = 1, /* FP32 arithmetic (force, kicks, link update, projection) on links and E-field
+                               stored as compensated FP32 pairs (hi + lo, error-free two-sum updates);
+                               Hamiltonian, Delta H, plaquette and residual sums in FP64; Delta H from
+                               difference kernels; reprojection in FP64 */
+    LQ_PRECISION_F32 = 2    /* as MIXED but links and E-field stored as plain FP32 (half the bytes,
+                               Delta H error grows with the volume) */
 };
 
 /* SymplecticIntegrator methods (src/integrator/mod.rs:93-208) */
@@ -176,8 +181,8 @@ int lq_hmc_trajectory(lq_state *s, double dt, int n_steps, uint64_t seed, uint64
  * the state is bracketed by an event pair; totals accumulate at each synchronisation. */
 enum lq_kernel_class {
     LQ_KERNEL_MD = 0,         /* fused force/kick/drift (k_md) */
-    LQ_KERNEL_GAUSS = 1,      /* Gauss law G(x) + residual partials (k_gauss) */
-    LQ_KERNEL_GAUSS_STEP = 2, /* projection step (k_gauss_step) */
+    LQ_KERNEL_GAUSS = 1,       /* Gauss law G(x) + residual partials (k_gauss) */
+    LQ_KERNEL_GAUSS_SWEEP = 2, /* projection sweep fused with the next Gauss law (k_gauss_sweep) */
     LQ_KERNEL_PLAQUETTE = 3,  /* plaquette / hamiltonian_links partials (k_plaquette) */
     LQ_KERNEL_REDUCE = 4,     /* sum of squares and final reductions */
     LQ_KERNEL_OTHER = 5,      /* layout conversion, initialisation, reprojection */

@@ -1,4 +1,4 @@
-// engine.cuh -- launch wrappers of the device kernels for one (D, T) instantiation.
+// engine.cuh -- launch wrappers of the device kernels for one (D, T, COMP) instantiation.
 #pragma once
 #include <math.h>
 
@@ -7,7 +7,7 @@
 
 namespace lq {
 
-template <int D, typename T> struct Engine {
+template <int D, typename T, bool COMP> struct Engine {
     static Geo<D> geo(const State &s) {
         Geo<D> g;
         g.V = s.V;
@@ -22,58 +22,64 @@ template <int D, typename T> struct Engine {
     static dim3 link_grid(const State &s, int threads) { return dim3((s.V + threads - 1) / threads, D, 1); }
 
     static cudaError_t links_from_aos(State &s, const double *d_aos, void *dst) {
-        k_links_from_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (V2<T> *)dst, s.V);
+        k_links_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (V2<T> *)dst, s.V);
         return cudaGetLastError();
     }
     static cudaError_t links_to_aos(State &s, const void *src, double *d_aos) {
-        k_links_to_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)src, d_aos, s.V);
+        k_links_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)src, d_aos, s.V);
         return cudaGetLastError();
     }
     static cudaError_t links_cold(State &s, void *dst) {
         k_links_identity<T><<<1024, 256, 0, s.stream>>>((V2<T> *)dst, (size_t)s.V, D);
-        return cudaGetLastError();
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess && COMP)
+            e = cudaMemsetAsync((char *)dst + s.link_bytes() / 2, 0, s.link_bytes() / 2, s.stream);
+        return e;
     }
     static cudaError_t links_random(State &s, void *dst, uint64_t seed) {
         const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-        k_links_random<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, s.V, key);
+        k_links_random<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, s.V, key);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        k_normalize<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, geo(s));
+        k_normalize<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, geo(s));
         return cudaGetLastError();
     }
     static cudaError_t efield_from_aos(State &s, const double *d_aos) {
-        k_efield_from_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V);
+        k_efield_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V);
         return cudaGetLastError();
     }
     static cudaError_t efield_to_aos(State &s, double *d_aos) {
-        k_efield_to_aos<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)s.E, d_aos, s.V);
+        k_efield_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)s.E, d_aos, s.V);
         return cudaGetLastError();
     }
     static cudaError_t efield_normal(State &s, uint64_t seed, uint64_t counter, double sd) {
         const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-        k_efield_normal<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((T *)s.E, s.V, key, (uint32_t)counter,
-                                                                         (uint32_t)(counter >> 32), (T)sd);
+        k_efield_normal<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(
+            (T *)s.E, s.V, key, (uint32_t)counter, (uint32_t)(counter >> 32), (T)sd);
         return cudaGetLastError();
     }
-    static cudaError_t md(State &s, const void *Uin, void *Uout, int mode, double h1, double h2, double dt) {
+    static cudaError_t md(State &s, const void *Uin, void *Uout, const void *Ein, void *Eout, int mode, double h1,
+                          double h2, double dt) {
         // kick coefficient h * c_e / size with c_e = -sqrt(2 / C_A), C_A = 3
         const double ce = -sqrt(2.0 / 3.0) / s.size;
         // drift coefficient dt * sqrt(2 C_A) / size
         const double cu = sqrt(2.0 * 3.0) / s.size * dt;
         const T k1 = (T)(h1 * ce), k2 = (T)(h2 * ce), drift = (T)cu;
         const Geo<D> g = geo(s);
-        const dim3 grid = link_grid(s, 128);
+        const dim3 grid(((s.V + 127) / 128) * D, 1, 1); // mu fastest, see k_md
         const V2<T> *in = (const V2<T> *)Uin;
         V2<T> *out = (V2<T> *)Uout;
-        T *E = (T *)s.E;
+        const T *ei = (const T *)Ein;
+        T *eo = (T *)Eout;
         switch (mode) {
-        case MD_KICK: k_md<D, T, MD_KICK><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift); break;
-        case MD_DRIFT: k_md<D, T, MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift); break;
+        case MD_KICK: k_md<D, T, COMP, MD_KICK><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
+        case MD_DRIFT: k_md<D, T, COMP, MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
         case MD_KICK | MD_DRIFT:
-            k_md<D, T, MD_KICK | MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift);
+            k_md<D, T, COMP, MD_KICK | MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift);
             break;
         case MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E:
-            k_md<D, T, MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E><<<grid, 128, 0, s.stream>>>(in, out, E, g, k1, k2, drift);
+            k_md<D, T, COMP, MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E>
+                <<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift);
             break;
         default: return cudaErrorInvalidValue;
         }
@@ -85,9 +91,11 @@ template <int D, typename T> struct Engine {
         *n_partials = blocks;
         return cudaGetLastError();
     }
-    static cudaError_t gauss_step(State &s, const void *U) {
-        k_gauss_step<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)U, (T *)s.E, (const T *)s.G,
-                                                                       geo(s));
+    static cudaError_t gauss_sweep(State &s, const void *U, uint32_t *n_partials) {
+        const uint32_t blocks = (s.V + 127) / 128;
+        k_gauss_sweep<D, T, COMP><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.E_alt,
+                                                                 (const T *)s.G, (T *)s.G_alt, geo(s), s.partial);
+        *n_partials = blocks;
         return cudaGetLastError();
     }
     static cudaError_t gauss_to_aos(State &s, double *d_out) {
@@ -100,14 +108,28 @@ template <int D, typename T> struct Engine {
         *n_partials = blocks;
         return cudaGetLastError();
     }
-    static cudaError_t efield_sumsq(State &s, uint32_t *n_partials) {
+    static cudaError_t plaquette_delta(State &s, const void *Uold, const void *Unew, uint32_t *n_partials) {
+        const uint32_t blocks = (s.V + 127) / 128;
+        k_plaquette_delta<D, T, COMP>
+            <<<blocks, 128, 0, s.stream>>>((const V2<T> *)Uold, (const V2<T> *)Unew, geo(s), s.partial);
+        *n_partials = blocks;
+        return cudaGetLastError();
+    }
+    static cudaError_t efield_sumsq(State &s, const void *E, uint32_t *n_partials) {
         const uint32_t blocks = 1024;
-        k_sum_squares<T><<<blocks, 256, 0, s.stream>>>((const T *)s.E, s.efield_elems(), s.partial);
+        k_sum_squares<T, COMP><<<blocks, 256, 0, s.stream>>>((const T *)E, s.efield_elems(), s.partial);
+        *n_partials = blocks;
+        return cudaGetLastError();
+    }
+    static cudaError_t efield_sumsq_delta(State &s, const void *Eold, const void *Enew, uint32_t *n_partials) {
+        const uint32_t blocks = 1024;
+        k_sum_squares_delta<T, COMP>
+            <<<blocks, 256, 0, s.stream>>>((const T *)Eold, (const T *)Enew, s.efield_elems(), s.partial);
         *n_partials = blocks;
         return cudaGetLastError();
     }
     static cudaError_t normalize(State &s, void *U) {
-        k_normalize<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)U, geo(s));
+        k_normalize<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)U, geo(s));
         return cudaGetLastError();
     }
     static cudaError_t finalize(State &s, int nv, uint32_t n, int offset) {
@@ -120,9 +142,10 @@ template <int D, typename T> struct Engine {
     }
 
     static const Ops *table() {
-        static const Ops ops = {links_from_aos, links_to_aos, links_cold,   links_random, efield_from_aos,
-                                efield_to_aos,  efield_normal, md,          gauss,        gauss_step,
-                                gauss_to_aos,   plaquette,     efield_sumsq, normalize,    finalize};
+        static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
+                                efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
+                                gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
+                                normalize,      finalize};
         return &ops;
     }
 };

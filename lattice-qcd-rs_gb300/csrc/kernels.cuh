@@ -1,9 +1,12 @@
 // kernels.cuh -- device kernels of the HMC molecular-dynamics path, templated on the
-// lattice dimension D (2, 3, 4) and the storage/compute type T (double or float).
+// lattice dimension D (2, 3, 4), the arithmetic type T (double or float) and COMP, which
+// selects compensated storage: every stored real is a pair (hi, lo) of T, hi + lo, updated
+// with error-free two-sums, while all products use hi only.
 //
 // Device layout (structure of arrays, one plane per matrix/vector component):
 //   links  U : vec2<T>[D][9][V]   U[(mu*9 + k)*V + site], k = row*3 + col
-//   efield E : T[D][8][V]          E[(mu*8 + a)*V + site]
+//              with COMP, the lo planes follow:  U[D*9*V + (mu*9 + k)*V + site]
+//   efield E : T[D][8][V]          E[(mu*8 + a)*V + site]   (+ lo planes at D*8*V)
 //   gauss  G : T[9][V]             Hermitian G(x): real diagonal + upper off-diagonal
 // Sites are linearised x_0 fastest as in the reference (src/lattice.rs:909-916), so the
 // +-mu neighbour of a site is +-L^mu with periodic wrap, and consecutive threads touch
@@ -34,6 +37,23 @@ __device__ __forceinline__ uint32_t bwd(const Geo<D> &g, uint32_t site, uint32_t
 }
 
 template <typename T> using V2 = typename vec2_t<T>::type;
+
+// (hi, lo) += d: two-sum of hi and d, error folded into lo, pair renormalised
+// (Knuth's TwoSum followed by Dekker's FastTwoSum; no product, so nothing is contracted).
+template <typename T> __device__ __forceinline__ void comp_add(T &hi, T &lo, T d) {
+    const T s = hi + d;
+    const T bb = s - hi;
+    const T err = (hi - (s - bb)) + (d - bb);
+    const T l = lo + err;
+    const T h = s + l;
+    lo = l - (h - s);
+    hi = h;
+}
+// split a double into a pair of T (exact for T = double with lo = 0)
+template <typename T> __device__ __forceinline__ void split(double x, T &hi, T &lo) {
+    hi = (T)x;
+    lo = (T)(x - (double)hi);
+}
 
 // ------------------------------------------------------------------ block reductions
 // Fixed-shape warp-shuffle + shared-memory tree: deterministic for a given launch shape.
@@ -72,10 +92,7 @@ __global__ void __launch_bounds__(1024) k_finalize(const double *__restrict__ pa
         for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) s += partial[(size_t)i * n + k];
         v[i] = s;
     }
-    double tmp[NV];
-#pragma unroll
-    for (int i = 0; i < NV; ++i) tmp[i] = v[i];
-    block_reduce_store<NV>(tmp, out, 0, 1);
+    block_reduce_store<NV>(v, out, 0, 1);
 }
 
 // ------------------------------------------------------------------ gauge force
@@ -114,56 +131,81 @@ __device__ __forceinline__ void staple_sum(const V2<T> *__restrict__ U, const Ge
 
 enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4 };
 
-// One thread per link (site = x index, mu = blockIdx.y).
+// One thread per link.  Blocks are ordered with mu fastest (blockIdx.x = site_block*D + mu)
+// so the D directions of a block of sites run together and the neighbour links they share
+// stay in L2.
 //  KICK : F^a = Im Tr(T^a U_mu(x) Sigma(x)) (derivative_e, src/simulation/state.rs:1420-1448);
 //         e += k1 * F (when k1 != 0), then e += k2 * F, with k = h * c_e / size,
 //         c_e = -sqrt(2/C_A).  Two separate adds keep the reference's rounding of a step end
 //         followed by the next step's start (src/integrator/symplectic_euler_rayon.rs:222-252).
+//         E is read from Ein and written to Eout (the same buffer for an in-place update).
 //  DRIFT: U' = U + drift * i (E U), drift = dt sqrt(2 C_A) / size
 //         (derivative_u + integrate_link, src/simulation/state.rs:1407-1417,
 //          src/integrator/mod.rs:216-233), with E after the kick or, with DRIFT_OLD_E,
 //         before it (integrate_sync_sync integrates both fields from the old state).
-template <int D, typename T, int MODE>
-__global__ void __launch_bounds__(128) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout,
-                                            T *__restrict__ E, Geo<D> g, T k1, T k2, T drift) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    const int mu = blockIdx.y;
+template <int D, typename T, bool COMP, int MODE>
+__global__ void __launch_bounds__(128) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein,
+                                            T *Eout, Geo<D> g, T k1, T k2, T drift) {
+    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.x % D;
     if (site >= g.V) return;
     const size_t V = g.V;
+    const size_t elo = (size_t)D * 8 * V, ulo = (size_t)D * 9 * V;
     uint32_t c[D];
     site_coords(g, site, c);
-    T e[8];
+    T e[8], el[8], e_old[8];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) e[a] = E[(size_t)(mu * 8 + a) * V + site];
+    for (int a = 0; a < 8; ++a) {
+        e[a] = Ein[(size_t)(mu * 8 + a) * V + site];
+        el[a] = COMP ? Ein[elo + (size_t)(mu * 8 + a) * V + site] : T(0);
+        e_old[a] = e[a];
+    }
     mat3<T> u;
     load_link<T>(Uin, (size_t)(mu * 9) * V, V, site, u);
-    T e_old[8];
-#pragma unroll
-    for (int a = 0; a < 8; ++a) e_old[a] = e[a];
     if (MODE & MD_KICK) {
         mat3<T> sig, m;
         staple_sum<D, T>(Uin, g, site, c, mu, sig);
         mul_nn(u, sig, m);
         T f[8];
         im_tr_generators(m, f);
-        if (k1 != T(0)) {
-#pragma unroll
-            for (int a = 0; a < 8; ++a) e[a] = fma(k1, f[a], e[a]);
-        }
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
-            e[a] = fma(k2, f[a], e[a]);
-            E[(size_t)(mu * 8 + a) * V + site] = e[a];
+            if (COMP) {
+                if (k1 != T(0)) comp_add(e[a], el[a], k1 * f[a]);
+                comp_add(e[a], el[a], k2 * f[a]);
+                Eout[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
+            } else {
+                if (k1 != T(0)) e[a] = fma(k1, f[a], e[a]);
+                e[a] = fma(k2, f[a], e[a]);
+            }
+            Eout[(size_t)(mu * 8 + a) * V + site] = e[a];
+        }
+    } else if (Eout != Ein) {
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            Eout[(size_t)(mu * 8 + a) * V + site] = e[a];
+            if (COMP) Eout[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
         }
     }
     if (MODE & MD_DRIFT) {
         mat3<T> em, w;
         adjoint_to_matrix<T>((MODE & MD_DRIFT_OLD_E) ? e_old : e, em);
         mul_nn(em, u, w);
+        if (COMP) {
+            mat3<T> ul;
+            load_link<T>(Uin + ulo, (size_t)(mu * 9) * V, V, site, ul);
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            u.e[k].re = fma(-drift, w.e[k].im, u.e[k].re);
-            u.e[k].im = fma(drift, w.e[k].re, u.e[k].im);
+            for (int k = 0; k < 9; ++k) {
+                comp_add(u.e[k].re, ul.e[k].re, -drift * w.e[k].im);
+                comp_add(u.e[k].im, ul.e[k].im, drift * w.e[k].re);
+            }
+            store_link<T>(Uout + ulo, (size_t)(mu * 9) * V, V, site, ul);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                u.e[k].re = fma(-drift, w.e[k].im, u.e[k].re);
+                u.e[k].im = fma(drift, w.e[k].re, u.e[k].im);
+            }
         }
         store_link<T>(Uout, (size_t)(mu * 9) * V, V, site, u);
     }
@@ -207,7 +249,7 @@ template <typename T> __device__ __forceinline__ void herm_store(T *__restrict__
 // G(x) = sum_mu [E_mu(x) - U_mu(x-mu)^dag E_mu(x-mu) U_mu(x-mu)]  (EField::gauss,
 // src/field.rs:1174-1195); the per-site residual |Tr((sum_a T^a) G(x))| = |sum_a g^a| / 2,
 // g^a = 2 Re Tr(T^a G) (gauss_sum_div, src/field.rs:1199-1220), is reduced into one
-// partial per block.
+// partial per block.  Reads hi parts only.
 template <int D, typename T>
 __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, const T *__restrict__ E,
                                                T *__restrict__ G, Geo<D> g, double *__restrict__ partial) {
@@ -243,10 +285,10 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
         herm_store(G, V, site, gs);
         T gc[8];
         two_re_tr_generators(gs, gc);
-        double s = 0.0;
+        T s = T(0);
 #pragma unroll
-        for (int a = 0; a < 8; ++a) s += (double)gc[a];
-        r[0] = fabs(s) * 0.5;
+        for (int a = 0; a < 8; ++a) s += gc[a];
+        r[0] = (double)(fabs(s) * T(0.5));
     }
     block_reduce_store<1>(r, partial, blockIdx.x, gridDim.x);
 }
@@ -254,33 +296,105 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
 // One projection step on link (x, mu) (EField::project_to_gauss_step, src/field.rs:1301-1337):
 //   e'^a = 2 Re Tr(T^a [(u G(x) u^dag G(x+mu) - G(x)) K + T^a e^a]),  K = 0.12
 //        = e^a + K (2 Re Tr(T^a u G(x) u^dag G(x+mu)) - 2 Re Tr(T^a G(x)))
-// E is updated in place: each thread reads and writes only its own link.
-template <int D, typename T>
-__global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U, T *__restrict__ E,
-                                                    const T *__restrict__ G, Geo<D> g) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    const int mu = blockIdx.y;
-    if (site >= g.V) return;
-    const size_t V = g.V;
-    uint32_t c[D];
-    site_coords(g, site, c);
-    const uint32_t xp = fwd(g, site, c[mu], mu);
-    mat3<T> u, gm, gpm, t1, t2, x;
-    herm_load(G, V, site, gm);
-    herm_load(G, V, xp, gpm);
-    load_link<T>(U, (size_t)(mu * 9) * V, V, site, u);
-    mul_nn(u, gm, t1);
+// with u = U_mu(x).  One function serves both call sites of k_gauss_sweep so that the
+// recomputed update of a neighbour's link is the same arithmetic as its owner's.
+template <typename T, bool COMP>
+__device__ __forceinline__ void projection_step(const mat3<T> &u, const mat3<T> &gx, const T *gxc, const mat3<T> &gp,
+                                                T *e, T *el) {
+    mat3<T> t1, t2, x;
+    mul_nn(u, gx, t1);
     mul_na(t1, u, t2);
-    mul_nn(t2, gpm, x);
-    T xc[8], gc[8];
+    mul_nn(t2, gp, x);
+    T xc[8];
     two_re_tr_generators(x, xc);
-    two_re_tr_generators(gm, gc);
     const T K = T(0.12);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        const size_t idx = (size_t)(mu * 8 + a) * V + site;
-        E[idx] = fma(K, xc[a] - gc[a], E[idx]);
+        if (COMP) comp_add(e[a], el[a], K * (xc[a] - gxc[a]));
+        else e[a] = fma(K, xc[a] - gxc[a], e[a]);
     }
+}
+
+// One projection sweep fused with the Gauss law of its result, one thread per site x:
+//   E'_mu(x)    = step(U_mu(x),    G(x),    G(x+mu), E_mu(x))      written to Eout
+//   E'_mu(x-mu) = step(U_mu(x-mu), G(x-mu), G(x),    E_mu(x-mu))   recomputed, not written
+//   G'(x) = sum_mu [E'_mu(x) - U_mu(x-mu)^dag E'_mu(x-mu) U_mu(x-mu)]   written to Gout
+// plus the residual partials of G'.  E and G are double-buffered (a thread reads its
+// neighbours' old values while they are being replaced).  U is read once per sweep instead
+// of twice (Gauss law, then step) and the sweep needs one launch instead of two.
+template <int D, typename T, bool COMP>
+__global__ void __launch_bounds__(128) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
+                                                     T *__restrict__ Eout, const T *__restrict__ Gin,
+                                                     T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double r[1] = {0.0};
+    if (site < g.V) {
+        const size_t V = g.V;
+        const size_t elo = (size_t)D * 8 * V;
+        uint32_t c[D];
+        site_coords(g, site, c);
+        mat3<T> gx, gnew;
+        herm_load(Gin, V, site, gx);
+        T gxc[8];
+        two_re_tr_generators(gx, gxc);
+        mat_zero(gnew);
+#pragma unroll
+        for (int mu = 0; mu < D; ++mu) {
+            T e[8], el[8];
+            {
+                mat3<T> u, gp, em;
+                load_link<T>(U, (size_t)(mu * 9) * V, V, site, u);
+                herm_load(Gin, V, fwd(g, site, c[mu], mu), gp);
+#pragma unroll
+                for (int a = 0; a < 8; ++a) {
+                    e[a] = Ein[(size_t)(mu * 8 + a) * V + site];
+                    el[a] = COMP ? Ein[elo + (size_t)(mu * 8 + a) * V + site] : T(0);
+                }
+                projection_step<T, COMP>(u, gx, gxc, gp, e, el);
+#pragma unroll
+                for (int a = 0; a < 8; ++a) {
+                    Eout[(size_t)(mu * 8 + a) * V + site] = e[a];
+                    if (COMP) Eout[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
+                }
+                adjoint_to_matrix<T>(e, em);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    gnew.e[k].re += em.e[k].re;
+                    gnew.e[k].im += em.e[k].im;
+                }
+            }
+            {
+                const uint32_t xm = bwd(g, site, c[mu], mu);
+                mat3<T> w, gm, em, t, wm;
+                load_link<T>(U, (size_t)(mu * 9) * V, V, xm, w);
+                herm_load(Gin, V, xm, gm);
+                T gmc[8];
+                two_re_tr_generators(gm, gmc);
+#pragma unroll
+                for (int a = 0; a < 8; ++a) {
+                    e[a] = Ein[(size_t)(mu * 8 + a) * V + xm];
+                    el[a] = COMP ? Ein[elo + (size_t)(mu * 8 + a) * V + xm] : T(0);
+                }
+                projection_step<T, COMP>(w, gm, gmc, gx, e, el);
+                adjoint_to_matrix<T>(e, em);
+                mul_nn(em, w, t);
+                mul_an(w, t, wm);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    gnew.e[k].re -= wm.e[k].re;
+                    gnew.e[k].im -= wm.e[k].im;
+                }
+            }
+        }
+        herm_store(Gout, V, site, gnew);
+        T gc[8];
+        two_re_tr_generators(gnew, gc);
+        T sum = T(0);
+#pragma unroll
+        for (int a = 0; a < 8; ++a) sum += gc[a];
+        r[0] = (double)(fabs(sum) * T(0.5));
+    }
+    block_reduce_store<1>(r, partial, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ plaquettes
@@ -288,8 +402,8 @@ __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U,
 // (pij, src/field.rs:761-771), Tr P = Tr(A B^dag) with A = U_mu(x) U_nu(x+mu),
 // B = U_nu(x) U_mu(x+nu).  Partials: [0] sum (1 - Re Tr P / 3) (hamiltonian_links,
 // src/simulation/state.rs:821-849), [1] sum Re Tr P, [2] sum Im Tr P
-// (average_trace_plaquette, src/field.rs:775-804); the per-plaquette traces are in T and
-// every sum is in double.
+// (average_trace_plaquette, src/field.rs:775-804).  The traces of one site accumulate in
+// T (hi parts of compensated links) and every sum over sites in double.
 template <int D, typename T>
 __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, Geo<D> g,
                                                    double *__restrict__ partial) {
@@ -299,6 +413,7 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
         const size_t V = g.V;
         uint32_t c[D];
         site_coords(g, site, c);
+        T sre = T(0), sim = T(0), sh = T(0);
 #pragma unroll
         for (int mu = 0; mu < D; ++mu) {
             const uint32_t xpmu = fwd(g, site, c[mu], mu);
@@ -319,37 +434,148 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
                     im = fma(A.e[k].im, B.e[k].re, im);
                     im = fma(-A.e[k].re, B.e[k].im, im);
                 }
-                v[0] += 1.0 - (double)re / 3.0;
-                v[1] += (double)re;
-                v[2] += (double)im;
+                sh += T(1) - re / T(3);
+                sre += re;
+                sim += im;
             }
         }
+        v[0] = (double)sh;
+        v[1] = (double)sre;
+        v[2] = (double)sim;
     }
     block_reduce_store<3>(v, partial, blockIdx.x, gridDim.x);
 }
 
-// sum of squares of n values (hamiltonian_efield before the beta/2 factor), in double
-template <typename T>
-__global__ void __launch_bounds__(256) k_sum_squares(const T *__restrict__ x, size_t n, double *__restrict__ partial) {
+// Difference of the plaquette sums of two link fields, Re Tr[P(U') - P(U)] summed over
+// every plaquette, evaluated without cancellation: with P = A B C^dag Dd^dag
+// (A = U_mu(x), B = U_nu(x+mu), C = U_mu(x+nu), Dd = U_nu(x)) the exact telescoping
+//   P' - P = dA B' C'^dag Dd'^dag + A dB C'^dag Dd'^dag + A B dC^dag Dd'^dag + A B C^dag dDd^dag
+// needs only products with one difference factor, so FP32 products leave an error
+// proportional to |dU|, not to |U|.  dU = (hi' - hi) + (lo' - lo) keeps the compensated part.
+// Partial: sum Re Tr(P' - P) (Delta hamiltonian_links = -beta/3 times it).
+template <int D, typename T, bool COMP>
+__global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
+                                                         Geo<D> g, double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const double y = (double)x[i];
-        v[0] = fma(y, y, v[0]);
+    if (site < g.V) {
+        const size_t V = g.V;
+        const size_t ulo = (size_t)D * 9 * V;
+        uint32_t c[D];
+        site_coords(g, site, c);
+        auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
+            load_link<T>(Uo, (size_t)(dir * 9) * V, V, x, old_hi);
+            load_link<T>(Un, (size_t)(dir * 9) * V, V, x, new_hi);
+            if (COMP) {
+                mat3<T> ol, nl;
+                load_link<T>(Uo + ulo, (size_t)(dir * 9) * V, V, x, ol);
+                load_link<T>(Un + ulo, (size_t)(dir * 9) * V, V, x, nl);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    diff.e[k].re = (new_hi.e[k].re - old_hi.e[k].re) + (nl.e[k].re - ol.e[k].re);
+                    diff.e[k].im = (new_hi.e[k].im - old_hi.e[k].im) + (nl.e[k].im - ol.e[k].im);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    diff.e[k].re = new_hi.e[k].re - old_hi.e[k].re;
+                    diff.e[k].im = new_hi.e[k].im - old_hi.e[k].im;
+                }
+            }
+        };
+        // Re Tr(X Y) and Re Tr(X Y^dag)
+        auto re_tr_nn = [](const mat3<T> &x, const mat3<T> &y) {
+            T s = T(0);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    s = fma(x.e[i * 3 + k].re, y.e[k * 3 + i].re, s);
+                    s = fma(-x.e[i * 3 + k].im, y.e[k * 3 + i].im, s);
+                }
+            return s;
+        };
+        auto re_tr_na = [](const mat3<T> &x, const mat3<T> &y) {
+            T s = T(0);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                s = fma(x.e[k].re, y.e[k].re, s);
+                s = fma(x.e[k].im, y.e[k].im, s);
+            }
+            return s;
+        };
+        T acc = T(0);
+#pragma unroll
+        for (int mu = 0; mu < D; ++mu) {
+            const uint32_t xpmu = fwd(g, site, c[mu], mu);
+#pragma unroll
+            for (int nu = mu + 1; nu < D; ++nu) {
+                const uint32_t xpnu = fwd(g, site, c[nu], nu);
+                mat3<T> A, An, dA, B, Bn, dB, C, Cn, dC, Dd, Dn, dD, q1, s1, l1, t;
+                load_pair(mu, site, A, An, dA);
+                load_pair(nu, xpmu, B, Bn, dB);
+                load_pair(mu, xpnu, C, Cn, dC);
+                load_pair(nu, site, Dd, Dn, dD);
+                T term = T(0);
+                mul_nn(Dn, Cn, q1);       // Q1 = Dd' C'       (C'^dag Dd'^dag = Q1^dag)
+                mul_na(Bn, q1, s1);       // B' C'^dag Dd'^dag
+                term += re_tr_nn(dA, s1); // Tr(dA B' C'^dag Dd'^dag)
+                mul_an(q1, A, t);         // C'^dag Dd'^dag A
+                term += re_tr_nn(dB, t);  // Tr(A dB C'^dag Dd'^dag)
+                mul_nn(A, B, l1);         // L1 = A B
+                mul_an(Dn, l1, t);        // Dd'^dag A B
+                term += re_tr_na(t, dC);  // Tr(A B dC^dag Dd'^dag) = Re Tr((Dd'^dag A B) dC^dag)
+                mul_na(l1, C, t);         // A B C^dag
+                term += re_tr_na(t, dD);  // Tr(A B C^dag dDd^dag)
+                acc += term;
+            }
+        }
+        v[0] = (double)acc;
     }
     block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
 }
 
+// sum of squares of an E-field (hi + lo), hamiltonian_efield before the beta/2 factor
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(256) k_sum_squares(const T *__restrict__ x, size_t n, double *__restrict__ partial) {
+    T acc = T(0);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const T y = x[i];
+        if (COMP) acc = fma(y, y, fma(T(2) * y, x[n + i], acc));
+        else acc = fma(y, y, acc);
+    }
+    double v[1] = {(double)acc};
+    block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
+}
+
+// sum over E-field components of (e' - e)(e' + e), i.e. Delta of the sum of squares, with
+// e' - e including the compensated parts (Delta hamiltonian_efield = beta/2 times it)
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(256) k_sum_squares_delta(const T *__restrict__ eo, const T *__restrict__ en, size_t n,
+                                                           double *__restrict__ partial) {
+    T acc = T(0);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const T a = eo[i], b = en[i];
+        T d = b - a;
+        if (COMP) d += en[n + i] - eo[n + i];
+        acc = fma(d, a + b, acc);
+    }
+    double v[1] = {(double)acc};
+    block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
+}
+
 // ------------------------------------------------------------------ reprojection
-// orthonormalize_matrix (src/su3.rs:290-309), computed in double for either storage type:
+// orthonormalize_matrix (src/su3.rs:290-309), computed in double for every storage type:
 // v1 = col0 / |col0|, v2 = col1 - v1 (v1^* . col1), normalised, col2 = conj(v1) x conj(v2);
 // a vector whose norm is <= f64::EPSILON is kept unnormalised (try_normalize).
-template <int D, typename T>
+template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D> g) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= g.V) return;
     const size_t V = g.V;
     const size_t p0 = (size_t)(mu * 9) * V;
+    const size_t ulo = (size_t)D * 9 * V;
     double r1[3], i1[3], r2[3], i2[3];
 #pragma unroll
     for (int row = 0; row < 3; ++row) {
@@ -359,6 +585,14 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
         i1[row] = a.y;
         r2[row] = b.x;
         i2[row] = b.y;
+        if (COMP) {
+            const V2<T> al = U[ulo + p0 + (size_t)(row * 3 + 0) * V + site];
+            const V2<T> bl = U[ulo + p0 + (size_t)(row * 3 + 1) * V + site];
+            r1[row] += al.x;
+            i1[row] += al.y;
+            r2[row] += bl.x;
+            i2[row] += bl.y;
+        }
     }
     const double eps = 2.220446049250313e-16;
     double n1 = sqrt(r1[0] * r1[0] + i1[0] * i1[0] + r1[1] * r1[1] + i1[1] * i1[1] + r1[2] * r1[2] + i1[2] * i1[2]);
@@ -397,7 +631,6 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
-        // a_k1 b_k2 - a_k2 b_k1 with a = (r1, -i1), b = (r2, -i2)
         const double xr = r1[k1] * r2[k2] - i1[k1] * i2[k2];
         const double xi = -(r1[k1] * i2[k2] + i1[k1] * r2[k2]);
         const double yr = r1[k2] * r2[k1] - i1[k2] * i2[k1];
@@ -405,75 +638,96 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
         r3[k] = xr - yr;
         i3[k] = xi - yi;
     }
+    const double *cols_r[3] = {r1, r2, r3};
+    const double *cols_i[3] = {i1, i2, i3};
 #pragma unroll
-    for (int row = 0; row < 3; ++row) {
-        V2<T> a, b, cc;
-        a.x = (T)r1[row];
-        a.y = (T)i1[row];
-        b.x = (T)r2[row];
-        b.y = (T)i2[row];
-        cc.x = (T)r3[row];
-        cc.y = (T)i3[row];
-        U[p0 + (size_t)(row * 3 + 0) * V + site] = a;
-        U[p0 + (size_t)(row * 3 + 1) * V + site] = b;
-        U[p0 + (size_t)(row * 3 + 2) * V + site] = cc;
-    }
+    for (int row = 0; row < 3; ++row)
+#pragma unroll
+        for (int col = 0; col < 3; ++col) {
+            V2<T> h, l;
+            split(cols_r[col][row], h.x, l.x);
+            split(cols_i[col][row], h.y, l.y);
+            U[p0 + (size_t)(row * 3 + col) * V + site] = h;
+            if (COMP) U[ulo + p0 + (size_t)(row * 3 + col) * V + site] = l;
+        }
 }
 
 // ------------------------------------------------------------------ layout conversion
 // host serde layout (double AoS, column-major complex 3x3 per link) <-> device SoA planes
-template <int D, typename T>
+template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_links_from_aos(const double *__restrict__ aos, V2<T> *__restrict__ U,
                                                         uint32_t V) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     const double *src = aos + ((size_t)site * D + mu) * 18;
+    const size_t ulo = (size_t)D * 9 * V;
 #pragma unroll
     for (int col = 0; col < 3; ++col)
 #pragma unroll
         for (int row = 0; row < 3; ++row) {
-            V2<T> v;
-            v.x = (T)src[(col * 3 + row) * 2];
-            v.y = (T)src[(col * 3 + row) * 2 + 1];
-            U[(size_t)(mu * 9 + row * 3 + col) * V + site] = v;
+            V2<T> h, l;
+            split(src[(col * 3 + row) * 2], h.x, l.x);
+            split(src[(col * 3 + row) * 2 + 1], h.y, l.y);
+            const size_t idx = (size_t)(mu * 9 + row * 3 + col) * V + site;
+            U[idx] = h;
+            if (COMP) U[ulo + idx] = l;
         }
 }
-template <int D, typename T>
+template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ U, double *__restrict__ aos,
                                                       uint32_t V) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     double *dst = aos + ((size_t)site * D + mu) * 18;
+    const size_t ulo = (size_t)D * 9 * V;
 #pragma unroll
     for (int col = 0; col < 3; ++col)
 #pragma unroll
         for (int row = 0; row < 3; ++row) {
-            const V2<T> v = U[(size_t)(mu * 9 + row * 3 + col) * V + site];
-            dst[(col * 3 + row) * 2] = (double)v.x;
-            dst[(col * 3 + row) * 2 + 1] = (double)v.y;
+            const size_t idx = (size_t)(mu * 9 + row * 3 + col) * V + site;
+            const V2<T> v = U[idx];
+            double re = (double)v.x, im = (double)v.y;
+            if (COMP) {
+                const V2<T> l = U[ulo + idx];
+                re += (double)l.x;
+                im += (double)l.y;
+            }
+            dst[(col * 3 + row) * 2] = re;
+            dst[(col * 3 + row) * 2 + 1] = im;
         }
 }
-template <int D, typename T>
+template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restrict__ aos, T *__restrict__ E,
                                                          uint32_t V) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     const double *src = aos + ((size_t)site * D + mu) * 8;
+    const size_t elo = (size_t)D * 8 * V;
 #pragma unroll
-    for (int a = 0; a < 8; ++a) E[(size_t)(mu * 8 + a) * V + site] = (T)src[a];
+    for (int a = 0; a < 8; ++a) {
+        T h, l;
+        split(src[a], h, l);
+        E[(size_t)(mu * 8 + a) * V + site] = h;
+        if (COMP) E[elo + (size_t)(mu * 8 + a) * V + site] = l;
+    }
 }
-template <int D, typename T>
+template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, double *__restrict__ aos,
                                                        uint32_t V) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     double *dst = aos + ((size_t)site * D + mu) * 8;
+    const size_t elo = (size_t)D * 8 * V;
 #pragma unroll
-    for (int a = 0; a < 8; ++a) dst[a] = (double)E[(size_t)(mu * 8 + a) * V + site];
+    for (int a = 0; a < 8; ++a) {
+        double x = (double)E[(size_t)(mu * 8 + a) * V + site];
+        if (COMP) x += (double)E[elo + (size_t)(mu * 8 + a) * V + site];
+        dst[a] = x;
+    }
 }
 // G(x) as its 8 su(3) coefficients g^a = 2 Re Tr(T^a G(x))
 template <typename T>
@@ -488,6 +742,7 @@ __global__ void __launch_bounds__(256) k_gauss_to_aos(const T *__restrict__ G, d
     for (int a = 0; a < 8; ++a) out[(size_t)site * 8 + a] = (double)gc[a];
 }
 
+// identity links (hi planes; lo planes, when present, are cleared by the caller)
 template <typename T>
 __global__ void __launch_bounds__(256) k_links_identity(V2<T> *__restrict__ U, size_t V, int D) {
     const size_t n = V * 9 * D;
@@ -541,8 +796,9 @@ __device__ __forceinline__ void box_muller(float u1, float u2, float &z0, float 
     z1 = r * s;
 }
 
-// E^a(x, mu) ~ Normal(0, sd), independent per (link, a); counter = (link, ctr_lo, ctr_hi, call)
-template <int D, typename T>
+// E^a(x, mu) ~ Normal(0, sd), independent per (link, a); counter = (link, ctr_lo, ctr_hi, call).
+// FP64 states draw 53-bit uniforms and double-precision Box-Muller; FP32 states 24-bit ones.
+template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32_t V, uint2 key, uint32_t ctr_lo,
                                                        uint32_t ctr_hi, T sd) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
@@ -572,14 +828,18 @@ __global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32
             z[4 * j + 3] = (T)d2;
         }
     }
+    const size_t elo = (size_t)D * 8 * V;
 #pragma unroll
-    for (int a = 0; a < 8; ++a) E[(size_t)(mu * 8 + a) * V + site] = z[a] * sd;
+    for (int a = 0; a < 8; ++a) {
+        E[(size_t)(mu * 8 + a) * V + site] = z[a] * sd;
+        if (COMP) E[elo + (size_t)(mu * 8 + a) * V + site] = T(0);
+    }
 }
 
 // random_su3 (src/su3.rs:322-355) per link: two complex 3-vectors with Uniform(-1,1)
-// entries, redrawn while |v1| <= eps or |v1 . v2| <= eps, then Gram-Schmidt and
-// col2 = conj(v1) x conj(v2); computed in double, stored as T.
-template <int D, typename T>
+// entries, redrawn while |v1| <= eps or |v1 . v2| <= eps; written as columns 0 and 1, which
+// k_normalize then turns into Gram-Schmidt vectors and col2 = conj(v1) x conj(v2).
+template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uint32_t V, uint2 key) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
@@ -619,15 +879,20 @@ __global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uin
         if (hypot(dr, di) > eps) break;
     }
     const size_t p0 = (size_t)(mu * 9) * V;
+    const size_t ulo = (size_t)D * 9 * V;
 #pragma unroll
     for (int row = 0; row < 3; ++row) {
-        V2<T> a, b;
-        a.x = (T)r1[row];
-        a.y = (T)i1[row];
-        b.x = (T)r2[row];
-        b.y = (T)i2[row];
+        V2<T> a, b, al, bl;
+        split(r1[row], a.x, al.x);
+        split(i1[row], a.y, al.y);
+        split(r2[row], b.x, bl.x);
+        split(i2[row], b.y, bl.y);
         U[p0 + (size_t)(row * 3 + 0) * V + site] = a;
         U[p0 + (size_t)(row * 3 + 1) * V + site] = b;
+        if (COMP) {
+            U[ulo + p0 + (size_t)(row * 3 + 0) * V + site] = al;
+            U[ulo + p0 + (size_t)(row * 3 + 1) * V + site] = bl;
+        }
     }
 }
 

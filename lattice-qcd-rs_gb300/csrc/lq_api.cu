@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <utility>
 
 #include "kernels.cuh"
 #include "lqgpu.h"
@@ -94,6 +95,7 @@ void prof_free(State &s) {
     s.prof = nullptr;
 }
 
+// machine epsilon of the arithmetic of the state (the projection residual floor follows it)
 double eps_of(const State &s) { return s.precision == LQ_PRECISION_F64 ? 2.220446049250313e-16 : 1.1920928955078125e-07; }
 
 void free_state(State *s) {
@@ -102,7 +104,9 @@ void free_state(State *s) {
     for (int i = 0; i < 3; ++i)
         if (s->U[i]) cudaFree(s->U[i]);
     if (s->E) cudaFree(s->E);
+    if (s->E_alt) cudaFree(s->E_alt);
     if (s->G) cudaFree(s->G);
+    if (s->G_alt) cudaFree(s->G_alt);
     if (s->partial) cudaFree(s->partial);
     if (s->d_out) cudaFree(s->d_out);
     if (s->h_out) cudaFreeHost(s->h_out);
@@ -142,10 +146,10 @@ int plaquette_sums(State &s, const void *U, int offset) {
     LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->finalize(s, 3, n, offset));
     return LQ_OK;
 }
-// d_out[offset] <- sum of e^2
+// d_out[offset] <- sum of e^2 of the current E-field
 int efield_sumsq(State &s, int offset) {
     uint32_t n = 0;
-    LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->efield_sumsq(s, &n));
+    LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->efield_sumsq(s, s.E, &n));
     LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->finalize(s, 1, n, offset));
     return LQ_OK;
 }
@@ -155,36 +159,43 @@ int fetch_out(State &s, int count) {
     return LQ_OK;
 }
 
-// symplectic_n from U[src] (kept) into another buffer; returns the final buffer index.
-// E <- E + dt/2 F(U_k) (+ dt/2 F(U_k) of the next step) ...; U_{k+1} = U_k + dt dU(E, U_k)
-int run_symplectic(State &s, int src, int avoid, double dt, int n, int *final_buf) {
-    int a = other_buffer(s, src, avoid);
-    int b = other_buffer(s, src, a);
-    if (avoid >= 0 && b == avoid) b = src; // only two buffers usable: ping-pong through src
+// symplectic_n from U[src] (kept) into the other two buffers; returns the final buffer index.
+// E <- E + dt/2 F(U_k) (+ dt/2 F(U_k) of the next step) ...; U_{k+1} = U_k + dt dU(E, U_k).
+// With e_to_alt the first kick reads s.E and writes s.E_alt (later steps update s.E_alt in
+// place), so the start momenta survive in s.E.
+int run_symplectic(State &s, int src, double dt, int n, bool e_to_alt, int *final_buf) {
+    const int a = other_buffer(s, src, -1);
+    const int b = other_buffer(s, src, a);
+    void *ew = e_to_alt ? s.E_alt : s.E;
     const int KD = lq::MD_KICK | lq::MD_DRIFT;
-    LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[src], s.U[a], KD, 0.0, dt / 2.0, dt));
+    LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[src], s.U[a], s.E, ew, KD, 0.0, dt / 2.0, dt));
     int cur = a, nxt = b;
     for (int i = 1; i < n; ++i) {
-        LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[cur], s.U[nxt], KD, dt / 2.0, dt / 2.0, dt));
+        LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[cur], s.U[nxt], ew, ew, KD, dt / 2.0, dt / 2.0, dt));
         const int t = cur;
         cur = nxt;
         nxt = t;
     }
-    LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[cur], s.U[cur], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+    LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[cur], s.U[cur], ew, ew, lq::MD_KICK, 0.0, dt / 2.0, 0.0));
     *final_buf = cur;
     return LQ_OK;
 }
 
+// EField::project_to_gauss (src/field.rs:1265-1294): one step, then blocks of four steps
+// until the residual of the current field is <= eps * V * 320.  Each sweep also produces
+// G and the residual of its result, so the checks after steps 1, 5, 9, ... read it directly.
 int project_gauss(State &s, int max_steps, int *steps_done) {
     const double threshold = eps_of(s) * (double)((uint64_t)s.V * 4 * 8 * 10);
     const void *U = s.U[s.cur];
     uint32_t n = 0;
     int steps = 0;
     LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
-    LQ_LAUNCH(s, LQ_KERNEL_GAUSS_STEP, s.ops->gauss_step(s, U));
-    steps = 1;
     for (;;) {
-        LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+        LQ_LAUNCH(s, LQ_KERNEL_GAUSS_SWEEP, s.ops->gauss_sweep(s, U, &n));
+        std::swap(s.E, s.E_alt);
+        std::swap(s.G, s.G_alt);
+        ++steps;
+        if ((steps - 1) % 4 != 0) continue;
         LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->finalize(s, 1, n, 0));
         const int rc = fetch_out(s, 1);
         if (rc) return rc;
@@ -197,11 +208,6 @@ int project_gauss(State &s, int max_steps, int *steps_done) {
         if (max_steps > 0 && steps + 4 > max_steps) {
             if (steps_done) *steps_done = steps;
             return LQ_ERR_NOT_CONVERGED;
-        }
-        for (int k = 0; k < 4; ++k) {
-            if (k) LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
-            LQ_LAUNCH(s, LQ_KERNEL_GAUSS_STEP, s.ops->gauss_step(s, U));
-            ++steps;
         }
     }
     if (steps_done) *steps_done = steps;
@@ -248,7 +254,8 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
     if (size <= 0.0 || std::isnan(size) || std::isinf(size)) return LQ_ERR_NON_POSITIVE_SIZE;
     if (L < 2) return LQ_ERR_DIM_TOO_SMALL;
     if (dim < 2 || dim > 4) return LQ_ERR_UNSUPPORTED_DIM;
-    if (precision != LQ_PRECISION_F64 && precision != LQ_PRECISION_MIXED) return LQ_ERR_INVALID_ARGUMENT;
+    if (precision != LQ_PRECISION_F64 && precision != LQ_PRECISION_MIXED && precision != LQ_PRECISION_F32)
+        return LQ_ERR_INVALID_ARGUMENT;
     uint64_t V = 1;
     for (int i = 0; i < dim; ++i) {
         V *= (uint64_t)L;
@@ -269,7 +276,10 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
     s->beta = beta;
     s->precision = precision;
     s->real_bytes = precision == LQ_PRECISION_F64 ? 8 : 4;
-    s->ops = precision == LQ_PRECISION_F64 ? lq::ops_f64(dim) : lq::ops_f32(dim);
+    s->comp = precision == LQ_PRECISION_MIXED ? 1 : 0;
+    s->ops = precision == LQ_PRECISION_F64 ? lq::ops_f64(dim)
+             : precision == LQ_PRECISION_MIXED ? lq::ops_mixed(dim)
+                                               : lq::ops_f32(dim);
     s->partial_slots = lq::partial_slots_for(s->V);
     if (s->partial_slots < 1024) s->partial_slots = 1024;
     int rc = LQ_OK;
@@ -280,7 +290,9 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
     };
     for (int i = 0; i < 3; ++i) alloc(&s->U[i], s->link_bytes(), __LINE__);
     alloc(&s->E, s->efield_bytes(), __LINE__);
+    alloc(&s->E_alt, s->efield_bytes(), __LINE__);
     alloc(&s->G, s->gauss_bytes(), __LINE__);
+    alloc(&s->G_alt, s->gauss_bytes(), __LINE__);
     alloc((void **)&s->partial, sizeof(double) * 3 * (size_t)s->partial_slots, __LINE__);
     alloc((void **)&s->d_out, sizeof(double) * 16, __LINE__);
     if (!rc) {
@@ -362,7 +374,7 @@ int lq_state_set_beta(lq_state *s, double beta) {
 int lq_state_device_bytes(const lq_state *s, size_t *bytes) {
     LQ_CHECK_STATE(s);
     if (!bytes) return LQ_ERR_INVALID_ARGUMENT;
-    *bytes = 3 * s->link_bytes() + s->efield_bytes() + s->gauss_bytes() +
+    *bytes = 3 * s->link_bytes() + 2 * s->efield_bytes() + 2 * s->gauss_bytes() +
              sizeof(double) * (3 * (size_t)s->partial_slots + 16) + s->staging_bytes;
     return LQ_OK;
 }
@@ -560,7 +572,7 @@ int lq_integrate(lq_state *s, int mode, double dt, int n) {
     switch (mode) {
     case LQ_SYNC_SYNC:
         for (int i = 0; i < n; ++i) {
-            LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], KD | lq::MD_DRIFT_OLD_E, 0.0, dt, dt));
+            LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], st.E, st.E, KD | lq::MD_DRIFT_OLD_E, 0.0, dt, dt));
             const int t = a;
             a = b;
             b = t;
@@ -569,31 +581,31 @@ int lq_integrate(lq_state *s, int mode, double dt, int n) {
         st.t += n;
         break;
     case LQ_SYNC_LEAP:
-        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[a], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[a], st.E, st.E, lq::MD_KICK, 0.0, dt / 2.0, 0.0));
         st.leap = 1;
         break;
     case LQ_LEAP_LEAP:
-        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], lq::MD_DRIFT, 0.0, 0.0, dt));
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], st.E, st.E, lq::MD_DRIFT, 0.0, 0.0, dt));
         for (int i = 1; i < n; ++i) {
-            LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[a], KD, 0.0, dt, dt));
+            LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[a], st.E, st.E, KD, 0.0, dt, dt));
             const int t = a;
             a = b;
             b = t;
         }
-        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], lq::MD_KICK, 0.0, dt, 0.0));
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], st.E, st.E, lq::MD_KICK, 0.0, dt, 0.0));
         st.cur = b;
         st.t += n;
         break;
     case LQ_LEAP_SYNC:
-        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], lq::MD_DRIFT, 0.0, 0.0, dt));
-        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], st.E, st.E, lq::MD_DRIFT, 0.0, 0.0, dt));
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], st.E, st.E, lq::MD_KICK, 0.0, dt / 2.0, 0.0));
         st.cur = b;
         st.leap = 0;
         st.t += 1;
         break;
     default: { // LQ_SYMPLECTIC
         int fin = -1;
-        int rc = run_symplectic(st, st.cur, -1, dt, n, &fin);
+        int rc = run_symplectic(st, st.cur, dt, n, false, &fin);
         if (rc) return rc;
         st.cur = fin;
         st.t += n;
@@ -613,17 +625,17 @@ int lq_leapfrog_n(lq_state *s, double dt, int n) {
     const int KD = lq::MD_KICK | lq::MD_DRIFT;
     int a = st.cur, b = other_buffer(st, st.cur, -1);
     // sync -> leap: E += dt/2 F(U0)
-    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[a], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[a], st.E, st.E, lq::MD_KICK, 0.0, dt / 2.0, 0.0));
     // first drift (of leap_leap, or of leap_sync when n == 1)
-    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], lq::MD_DRIFT, 0.0, 0.0, dt));
+    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[a], st.U[b], st.E, st.E, lq::MD_DRIFT, 0.0, 0.0, dt));
     for (int i = 1; i < n; ++i) {
-        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[a], KD, 0.0, dt, dt));
+        LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[a], st.E, st.E, KD, 0.0, dt, dt));
         const int t = a;
         a = b;
         b = t;
     }
     // leap -> sync: E += dt/2 F(U_n)
-    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+    LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, st.U[b], st.U[b], st.E, st.E, lq::MD_KICK, 0.0, dt / 2.0, 0.0));
     st.cur = b;
     st.t += n;
     LQ_CK(sync_stream(st));
@@ -667,20 +679,41 @@ int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_
     rc = efield_sumsq(st, 3);
     if (rc) return rc;
     int fin = -1;
-    rc = run_symplectic(st, st.cur, -1, dt, n_steps, &fin);
+    rc = run_symplectic(st, st.cur, dt, n_steps, true, &fin); // start momenta stay in st.E
     if (rc) return rc;
-    // H of the proposal: d_out[4..6], d_out[7]
-    rc = plaquette_sums(st, st.U[fin], 4);
-    if (!rc) rc = efield_sumsq(st, 7);
-    if (!rc) rc = fetch_out(st, 8);
-    if (rc) return rc;
-    const double hu_old = st.hu_valid ? st.hu : st.h_out[0] * st.beta;
-    const double he_old = st.h_out[3] / 2.0 * st.beta;
-    const double hu_new = st.h_out[4] * st.beta;
-    const double he_new = st.h_out[7] / 2.0 * st.beta;
+    double hu_old = 0.0, he_old = 0.0, hu_new = 0.0, he_new = 0.0;
+    if (st.precision == LQ_PRECISION_F64) {
+        // probability_of_replacement (hybrid_monte_carlo.rs:584-589): both Hamiltonians summed
+        // separately, as the reference does; d_out[4..6], d_out[7]
+        std::swap(st.E, st.E_alt);
+        rc = plaquette_sums(st, st.U[fin], 4);
+        if (!rc) rc = efield_sumsq(st, 7);
+        if (!rc) rc = fetch_out(st, 8);
+        if (rc) return rc;
+        hu_old = st.hu_valid ? st.hu : st.h_out[0] * st.beta;
+        he_old = st.h_out[3] / 2.0 * st.beta;
+        hu_new = st.h_out[4] * st.beta;
+        he_new = st.h_out[7] / 2.0 * st.beta;
+    } else {
+        // FP32 arithmetic: Delta H from the difference kernels (no cancellation between two
+        // large sums); d_out[4] = sum Re Tr[P' - P], d_out[5] = sum (e' - e)(e' + e)
+        uint32_t n = 0;
+        LQ_LAUNCH(st, LQ_KERNEL_PLAQUETTE, st.ops->plaquette_delta(st, st.U[st.cur], st.U[fin], &n));
+        LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->finalize(st, 1, n, 4));
+        LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->efield_sumsq_delta(st, st.E, st.E_alt, &n));
+        LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->finalize(st, 1, n, 5));
+        rc = fetch_out(st, 6);
+        if (rc) return rc;
+        std::swap(st.E, st.E_alt);
+        hu_old = st.hu_valid ? st.hu : st.h_out[0] * st.beta;
+        he_old = st.h_out[3] / 2.0 * st.beta;
+        hu_new = hu_old - st.h_out[4] / 3.0 * st.beta;
+        he_new = he_old + st.h_out[5] / 2.0 * st.beta;
+    }
     const double h0 = hu_old + he_old, h1 = hu_new + he_new;
+    const double dh = (st.precision == LQ_PRECISION_F64) ? h1 - h0 : (hu_new - hu_old) + (he_new - he_old);
     // probability_of_replacement, hybrid_monte_carlo.rs:584-589 (NaN clamps to 1 as f64::min does)
-    double p = std::fmax(std::fmin(std::exp(h0 - h1), 1.0), 0.0);
+    double p = std::fmax(std::fmin(std::exp(-dh), 1.0), 0.0);
     if (prob) *prob = p;
     if (h_old) *h_old = h0;
     if (h_new) *h_new = h1;
@@ -688,6 +721,7 @@ int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_
     st.hu_valid = 1;
     st.pending_hu_old = hu_old;
     st.pending_hu_new = hu_new;
+    st.pending_dh = dh;
     st.pending_buf = fin;
     st.has_pending = 1;
     st.t = n_steps;
@@ -719,11 +753,12 @@ int lq_hmc_trajectory(lq_state *s, double dt, int n_steps, uint64_t seed, uint64
     rc = lq_hmc_propose(s, dt, n_steps, &p, &h0, &h1);
     if (rc) return rc;
     const int acc = (p >= 1.0 || uniform < p) ? 1 : 0;
+    const double dh = s->pending_dh;
     rc = lq_hmc_decide(s, acc);
     if (rc) return rc;
     if (accepted) *accepted = acc;
     if (prob) *prob = p;
-    if (delta_h) *delta_h = h1 - h0;
+    if (delta_h) *delta_h = dh;
     return LQ_OK;
 }
 

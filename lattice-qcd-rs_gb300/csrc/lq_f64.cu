@@ -4,9 +4,9 @@
 namespace lq {
 const Ops *ops_f64(int dim) {
     switch (dim) {
-    case 2: return Engine<2, double>::table();
-    case 3: return Engine<3, double>::table();
-    case 4: return Engine<4, double>::table();
+    case 2: return Engine<2, double, false>::table();
+    case 3: return Engine<3, double, false>::table();
+    case 4: return Engine<4, double, false>::table();
     default: return nullptr;
     }
 }

@@ -31,12 +31,15 @@ struct State {
     double beta = 1.0;
     int precision = LQ_PRECISION_F64;
     size_t real_bytes = 8; // sizeof(T)
+    int comp = 0;          // 1: compensated (hi, lo) storage of links and E-field
     cudaStream_t stream = nullptr;
 
     void *U[3] = {nullptr, nullptr, nullptr}; // link buffers (SoA); U[cur] is the state
     int cur = 0;
-    void *E = nullptr;   // E-field (SoA)
-    void *G = nullptr;   // Gauss-law matrix G(x), Hermitian, 9 reals per site
+    void *E = nullptr;     // E-field (SoA)
+    void *E_alt = nullptr; // second E buffer (projection sweeps are double-buffered)
+    void *G = nullptr;     // Gauss-law matrix G(x), Hermitian, 9 reals per site
+    void *G_alt = nullptr;
     double *partial = nullptr;
     uint32_t partial_slots = 0; // slots per row of `partial`
     double *d_out = nullptr;    // device scalars
@@ -50,7 +53,7 @@ struct State {
     // HMC proposal bookkeeping
     int has_pending = 0;
     int pending_buf = -1;
-    double pending_hu_old = 0.0, pending_hu_new = 0.0;
+    double pending_hu_old = 0.0, pending_hu_new = 0.0, pending_dh = 0.0;
     // cached hamiltonian_links of U[cur] (reductions are deterministic, so the cached value
     // equals a recomputation)
     int hu_valid = 0;
@@ -60,14 +63,14 @@ struct State {
     Prof *prof = nullptr; // non-null while profiling is enabled
 
     size_t link_elems() const { return (size_t)V * dim * 9; }   // complex elements
-    size_t link_bytes() const { return link_elems() * 2 * real_bytes; }
-    size_t efield_elems() const { return (size_t)V * dim * 8; } // reals
-    size_t efield_bytes() const { return efield_elems() * real_bytes; }
+    size_t link_bytes() const { return link_elems() * 2 * real_bytes * (comp ? 2 : 1); }
+    size_t efield_elems() const { return (size_t)V * dim * 8; } // reals (hi part)
+    size_t efield_bytes() const { return efield_elems() * real_bytes * (comp ? 2 : 1); }
     size_t gauss_bytes() const { return (size_t)V * 9 * real_bytes; }
 };
 
-// Device operations of one (D, T) instantiation.  Launches are asynchronous on s.stream
-// and return cudaError_t of the launch.
+// Device operations of one (D, T, COMP) instantiation.  Launches are asynchronous on
+// s.stream and return cudaError_t of the launch.
 struct Ops {
     cudaError_t (*links_from_aos)(State &s, const double *d_aos, void *dst);
     cudaError_t (*links_to_aos)(State &s, const void *src, double *d_aos);
@@ -76,15 +79,22 @@ struct Ops {
     cudaError_t (*efield_from_aos)(State &s, const double *d_aos);
     cudaError_t (*efield_to_aos)(State &s, double *d_aos);
     cudaError_t (*efield_normal)(State &s, uint64_t seed, uint64_t counter, double sd);
-    // md: mode bits MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E; h1, h2 kick step sizes; dt drift step
-    cudaError_t (*md)(State &s, const void *Uin, void *Uout, int mode, double h1, double h2, double dt);
+    // md: mode bits MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E; h1, h2 kick step sizes; dt drift step;
+    // E is read from Ein and written to Eout (equal for an in-place update)
+    cudaError_t (*md)(State &s, const void *Uin, void *Uout, const void *Ein, void *Eout, int mode, double h1,
+                      double h2, double dt);
     // gauss: G <- gauss(E, U), residual partials into s.partial (row 0), returns #partials
     cudaError_t (*gauss)(State &s, const void *U, uint32_t *n_partials);
-    cudaError_t (*gauss_step)(State &s, const void *U);
+    // one projection sweep E -> E_alt with G -> G_alt (= gauss(E_alt)) and its residual partials
+    cudaError_t (*gauss_sweep)(State &s, const void *U, uint32_t *n_partials);
     cudaError_t (*gauss_to_aos)(State &s, double *d_out);
     // plaquette partials (3 rows) of links buffer U, returns #partials
     cudaError_t (*plaquette)(State &s, const void *U, uint32_t *n_partials);
-    cudaError_t (*efield_sumsq)(State &s, uint32_t *n_partials);
+    // partials of sum Re Tr[P(Unew) - P(Uold)]
+    cudaError_t (*plaquette_delta)(State &s, const void *Uold, const void *Unew, uint32_t *n_partials);
+    cudaError_t (*efield_sumsq)(State &s, const void *E, uint32_t *n_partials);
+    // partials of sum (e_new - e_old)(e_new + e_old)
+    cudaError_t (*efield_sumsq_delta)(State &s, const void *Eold, const void *Enew, uint32_t *n_partials);
     cudaError_t (*normalize)(State &s, void *U);
     // finalize NV rows of n partials into d_out[offset..]
     cudaError_t (*finalize)(State &s, int nv, uint32_t n, int offset);
@@ -92,6 +102,7 @@ struct Ops {
 
 const Ops *ops_f64(int dim);
 const Ops *ops_f32(int dim);
+const Ops *ops_mixed(int dim);
 
 // partial slots needed for V sites
 inline uint32_t partial_slots_for(uint32_t V) { return (V + 127) / 128 + 64; }

@@ -30,6 +30,7 @@ globals().update({v: k for k, v in STATUS.items()})
 
 PRECISION_F64 = 0
 PRECISION_MIXED = 1
+PRECISION_F32 = 2
 SYNC_SYNC, SYNC_LEAP, LEAP_LEAP, LEAP_SYNC, SYMPLECTIC = range(5)
 
 # every symbol the header declares, with (restype, argtypes)
@@ -259,7 +260,7 @@ class State:
         _check(load().lq_leapfrog_n(self._h, dt, n), "lq_leapfrog_n")
 
     # ---- launch counters
-    KERNEL_CLASSES = ("md", "gauss", "gauss_step", "plaquette", "reduce", "other")
+    KERNEL_CLASSES = ("md", "gauss", "gauss_sweep", "plaquette", "reduce", "other")
 
     def profile_enable(self, on=True):
         _check(load().lq_profile_enable(self._h, 1 if on else 0), "lq_profile_enable")

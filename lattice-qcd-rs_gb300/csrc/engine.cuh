@@ -98,6 +98,11 @@ template <int D, typename T, bool COMP> struct Engine {
         *n_partials = blocks;
         return cudaGetLastError();
     }
+    static cudaError_t gauss_step(State &s, const void *U) {
+        const dim3 grid(((s.V + 127) / 128) * D, 1, 1);
+        k_gauss_step<D, T, COMP><<<grid, 128, 0, s.stream>>>((const V2<T> *)U, (T *)s.E, (const T *)s.G, geo(s));
+        return cudaGetLastError();
+    }
     static cudaError_t gauss_to_aos(State &s, double *d_out) {
         k_gauss_to_aos<T><<<(s.V + 255) / 256, 256, 0, s.stream>>>((const T *)s.G, d_out, s.V);
         return cudaGetLastError();
@@ -144,7 +149,7 @@ template <int D, typename T, bool COMP> struct Engine {
     static const Ops *table() {
         static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
                                 efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
-                                gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
+                                gauss_step,     gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
                                 normalize,      finalize};
         return &ops;
     }

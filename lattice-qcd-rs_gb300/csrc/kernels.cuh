@@ -38,6 +38,21 @@ __device__ __forceinline__ uint32_t bwd(const Geo<D> &g, uint32_t site, uint32_t
 
 template <typename T> using V2 = typename vec2_t<T>::type;
 
+// Minimum resident blocks per SM requested from the register allocator for the FP32 forms
+// of the MD kernel and the projection sweep (1: no request; 5 measured best on GB300 at
+// 32^4, about 96 registers).  The FP64 forms keep the
+// allocator's choice: their working set needs about twice the registers.
+#ifndef LQ_MD_MIN_BLOCKS
+#define LQ_MD_MIN_BLOCKS 5
+#endif
+#ifndef LQ_SWEEP_MIN_BLOCKS
+#define LQ_SWEEP_MIN_BLOCKS 5
+#endif
+template <typename T> struct MinBlocks {
+    static constexpr int md = sizeof(T) == 4 ? LQ_MD_MIN_BLOCKS : 1;
+    static constexpr int sweep = sizeof(T) == 4 ? LQ_SWEEP_MIN_BLOCKS : 1;
+};
+
 // (hi, lo) += d: two-sum of hi and d, error folded into lo, pair renormalised
 // (Knuth's TwoSum followed by Dekker's FastTwoSum; no product, so nothing is contracted).
 template <typename T> __device__ __forceinline__ void comp_add(T &hi, T &lo, T d) {
@@ -144,15 +159,23 @@ enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4 };
 //          src/integrator/mod.rs:216-233), with E after the kick or, with DRIFT_OLD_E,
 //         before it (integrate_sync_sync integrates both fields from the old state).
 template <int D, typename T, bool COMP, int MODE>
-__global__ void __launch_bounds__(128) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein,
-                                            T *Eout, Geo<D> g, T k1, T k2, T drift) {
+__global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout,
+                                  Geo<D> g, T k1, T k2, T drift) {
     const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
     const int mu = blockIdx.x % D;
     if (site >= g.V) return;
     const size_t V = g.V;
     const size_t elo = (size_t)D * 8 * V, ulo = (size_t)D * 9 * V;
-    uint32_t c[D];
-    site_coords(g, site, c);
+    // the staple sum first: the link and momenta of (x, mu) are loaded after it so they do
+    // not occupy registers while the neighbour links are in flight
+    mat3<T> sig;
+    if (MODE & MD_KICK) {
+        uint32_t c[D];
+        site_coords(g, site, c);
+        staple_sum<D, T>(Uin, g, site, c, mu, sig);
+    }
+    mat3<T> u;
+    load_link<T>(Uin, (size_t)(mu * 9) * V, V, site, u);
     T e[8], el[8], e_old[8];
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -160,11 +183,8 @@ __global__ void __launch_bounds__(128) k_md(const V2<T> *__restrict__ Uin, V2<T>
         el[a] = COMP ? Ein[elo + (size_t)(mu * 8 + a) * V + site] : T(0);
         e_old[a] = e[a];
     }
-    mat3<T> u;
-    load_link<T>(Uin, (size_t)(mu * 9) * V, V, site, u);
     if (MODE & MD_KICK) {
-        mat3<T> sig, m;
-        staple_sum<D, T>(Uin, g, site, c, mu, sig);
+        mat3<T> m;
         mul_nn(u, sig, m);
         T f[8];
         im_tr_generators(m, f);
@@ -315,6 +335,38 @@ __device__ __forceinline__ void projection_step(const mat3<T> &u, const mat3<T> 
     }
 }
 
+// One projection step on every link with G precomputed by k_gauss (the unfused form, used by
+// the FP64 state, whose arithmetic rate makes the sweep's recomputation too costly).  E is
+// updated in place: each thread reads and writes only its own link.
+template <int D, typename T, bool COMP>
+__global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U, T *__restrict__ E,
+                                                    const T *__restrict__ G, Geo<D> g) {
+    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.x % D;
+    if (site >= g.V) return;
+    const size_t V = g.V;
+    const size_t elo = (size_t)D * 8 * V;
+    uint32_t c[D];
+    site_coords(g, site, c);
+    mat3<T> u, gx, gp;
+    herm_load(G, V, site, gx);
+    herm_load(G, V, fwd(g, site, c[mu], mu), gp);
+    load_link<T>(U, (size_t)(mu * 9) * V, V, site, u);
+    T gxc[8], e[8], el[8];
+    two_re_tr_generators(gx, gxc);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        e[a] = E[(size_t)(mu * 8 + a) * V + site];
+        el[a] = COMP ? E[elo + (size_t)(mu * 8 + a) * V + site] : T(0);
+    }
+    projection_step<T, COMP>(u, gx, gxc, gp, e, el);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        E[(size_t)(mu * 8 + a) * V + site] = e[a];
+        if (COMP) E[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
+    }
+}
+
 // One projection sweep fused with the Gauss law of its result, one thread per site x:
 //   E'_mu(x)    = step(U_mu(x),    G(x),    G(x+mu), E_mu(x))      written to Eout
 //   E'_mu(x-mu) = step(U_mu(x-mu), G(x-mu), G(x),    E_mu(x-mu))   recomputed, not written
@@ -323,7 +375,7 @@ __device__ __forceinline__ void projection_step(const mat3<T> &u, const mat3<T> 
 // neighbours' old values while they are being replaced).  U is read once per sweep instead
 // of twice (Gauss law, then step) and the sweep needs one launch instead of two.
 template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
+__global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                                      T *__restrict__ Eout, const T *__restrict__ Gin,
                                                      T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;

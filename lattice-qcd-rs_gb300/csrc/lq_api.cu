@@ -189,11 +189,19 @@ int project_gauss(State &s, int max_steps, int *steps_done) {
     const void *U = s.U[s.cur];
     uint32_t n = 0;
     int steps = 0;
+    // FP32 arithmetic: one fused sweep per step (U read once).  FP64: the step and the Gauss
+    // law as two kernels, since the sweep's recomputed neighbour updates cost FP64 flops.
+    const bool fused = s.precision != LQ_PRECISION_F64;
     LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
     for (;;) {
-        LQ_LAUNCH(s, LQ_KERNEL_GAUSS_SWEEP, s.ops->gauss_sweep(s, U, &n));
-        std::swap(s.E, s.E_alt);
-        std::swap(s.G, s.G_alt);
+        if (fused) {
+            LQ_LAUNCH(s, LQ_KERNEL_GAUSS_SWEEP, s.ops->gauss_sweep(s, U, &n));
+            std::swap(s.E, s.E_alt);
+            std::swap(s.G, s.G_alt);
+        } else {
+            LQ_LAUNCH(s, LQ_KERNEL_GAUSS_SWEEP, s.ops->gauss_step(s, U));
+            LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+        }
         ++steps;
         if ((steps - 1) % 4 != 0) continue;
         LQ_LAUNCH(s, LQ_KERNEL_REDUCE, s.ops->finalize(s, 1, n, 0));

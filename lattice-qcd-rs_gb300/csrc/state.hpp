@@ -87,6 +87,8 @@ struct Ops {
     cudaError_t (*gauss)(State &s, const void *U, uint32_t *n_partials);
     // one projection sweep E -> E_alt with G -> G_alt (= gauss(E_alt)) and its residual partials
     cudaError_t (*gauss_sweep)(State &s, const void *U, uint32_t *n_partials);
+    // one projection step on E in place, from the G of the last gauss() call
+    cudaError_t (*gauss_step)(State &s, const void *U);
     cudaError_t (*gauss_to_aos)(State &s, double *d_out);
     // plaquette partials (3 rows) of links buffer U, returns #partials
     cudaError_t (*plaquette)(State &s, const void *U, uint32_t *n_partials);

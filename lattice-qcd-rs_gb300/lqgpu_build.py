@@ -37,8 +37,8 @@ def _deps():
     return max(os.path.getmtime(p) for p in paths)
 
 
-def _compile(src, extra):
-    obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+def _compile(src, extra, obj_dir):
+    obj = os.path.join(obj_dir, src.replace(".cu", ".o"))
     cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -46,25 +46,29 @@ def _compile(src, extra):
     return obj, r.stderr
 
 
-def build(force=False, verbose=False, extra=None):
-    """Compile and link; returns the path of the shared library."""
+def build(force=False, verbose=False, extra=None, out=None):
+    """Compile and link; returns the path of the shared library.  `extra` adds nvcc flags
+    (e.g. -D tuning knobs) and `out` names another output library for such a variant."""
     extra = list(extra or [])
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    if not force and not extra and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
-        return LIB
+    lib = out or LIB
+    obj_dir = os.path.join(BUILD_DIR, "obj_" + os.path.basename(lib).replace(".so", "")) if out else BUILD_DIR
+    os.makedirs(obj_dir, exist_ok=True)
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
+    if not force and not extra and os.path.exists(lib) and os.path.getmtime(lib) >= _deps():
+        return lib
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(lambda s: _compile(s, extra), SOURCES))
+        results = list(ex.map(lambda s: _compile(s, extra, obj_dir), SOURCES))
     if verbose:
         for _, err in results:
             if err:
                 sys.stderr.write(err)
-    tmp = LIB + ".tmp.%d" % os.getpid()
+    tmp = lib + ".tmp.%d" % os.getpid()
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + ["-lpthread", "-ldl", "-lrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -30,7 +30,7 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
     static cudaError_t links_cold(State &s, void *dst) {
-        k_links_identity<T><<<1024, 256, 0, s.stream>>>((V2<T> *)dst, (size_t)s.V, D);
+        k_links_identity<D, T><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, s.V);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess && COMP)
             e = cudaMemsetAsync((char *)dst + s.link_bytes() / 2, 0, s.link_bytes() / 2, s.stream);

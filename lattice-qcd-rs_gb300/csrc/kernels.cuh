@@ -3,14 +3,15 @@
 // selects compensated storage: every stored real is a pair (hi, lo) of T, hi + lo, updated
 // with error-free two-sums, while all products use hi only.
 //
-// Device layout (structure of arrays, one plane per matrix/vector component):
-//   links  U : vec2<T>[D][9][V]   U[(mu*9 + k)*V + site], k = row*3 + col
-//              with COMP, the lo planes follow:  U[D*9*V + (mu*9 + k)*V + site]
-//   efield E : T[D][8][V]          E[(mu*8 + a)*V + site]   (+ lo planes at D*8*V)
-//   gauss  G : T[9][V]             Hermitian G(x): real diagonal + upper off-diagonal
+// Device layout (tiled structure of arrays, see tix() in su3.cuh: 32-site tiles, all planes
+// of a tile contiguous, plane p of site s at ((s/32)*P + p)*32 + s%32):
+//   links  U : vec2<T>, P = D*9 planes, plane mu*9 + k holds entry k = row*3 + col of U_mu;
+//              with COMP the lo parts follow as a second array of the same shape
+//   efield E : T, P = D*8 planes, plane mu*8 + a holds e^a of E_mu (+ lo array with COMP)
+//   gauss  G : T, P = 9 planes, Hermitian G(x): real diagonal + upper off-diagonal
 // Sites are linearised x_0 fastest as in the reference (src/lattice.rs:909-916), so the
-// +-mu neighbour of a site is +-L^mu with periodic wrap, and consecutive threads touch
-// consecutive addresses of every plane (coalesced 128-bit/64-bit accesses).
+// +-mu neighbour of a site is +-L^mu with periodic wrap.  Arrays are padded to whole tiles;
+// padded sites are never written by the kernels and stay zero.
 #pragma once
 #include "su3.cuh"
 
@@ -118,7 +119,6 @@ __global__ void __launch_bounds__(1024) k_finalize(const double *__restrict__ pa
 template <int D, typename T>
 __device__ __forceinline__ void staple_sum(const V2<T> *__restrict__ U, const Geo<D> &g, uint32_t site,
                                            const uint32_t *c, int mu, mat3<T> &sig) {
-    const size_t V = g.V;
     const uint32_t xpmu = fwd(g, site, c[mu], mu);
     mat_zero(sig);
 #pragma unroll
@@ -126,19 +126,19 @@ __device__ __forceinline__ void staple_sum(const V2<T> *__restrict__ U, const Ge
         if (nu == mu) continue;
         {
             mat3<T> a, b, t;
-            load_link<T>(U, (size_t)(nu * 9) * V, V, xpmu, a);
-            load_link<T>(U, (size_t)(mu * 9) * V, V, fwd(g, site, c[nu], nu), b);
+            load_mat<T>(U + tix(xpmu, D * 9, nu * 9), a);
+            load_mat<T>(U + tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), b);
             mul_na(a, b, t);
-            load_link<T>(U, (size_t)(nu * 9) * V, V, site, a);
+            load_mat<T>(U + tix(site, D * 9, nu * 9), a);
             mul_na_acc(t, a, sig);
         }
         {
             mat3<T> a, b, w;
             const uint32_t xmnu = bwd(g, site, c[nu], nu);
-            load_link<T>(U, (size_t)(mu * 9) * V, V, xmnu, a);
-            load_link<T>(U, (size_t)(nu * 9) * V, V, bwd(g, xpmu, c[nu], nu), b);
+            load_mat<T>(U + tix(xmnu, D * 9, mu * 9), a);
+            load_mat<T>(U + tix(bwd(g, xpmu, c[nu], nu), D * 9, nu * 9), b);
             mul_nn(a, b, w);
-            load_link<T>(U, (size_t)(nu * 9) * V, V, xmnu, a);
+            load_mat<T>(U + tix(xmnu, D * 9, nu * 9), a);
             mul_an_acc(w, a, sig);
         }
     }
@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
     const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
     const int mu = blockIdx.x % D;
     if (site >= g.V) return;
-    const size_t V = g.V;
-    const size_t elo = (size_t)D * 8 * V, ulo = (size_t)D * 9 * V;
+    const size_t nt = tiles_of(g.V);
+    const size_t elo = nt * D * 8 * kTile, ulo = nt * D * 9 * kTile;
     // the staple sum first: the link and momenta of (x, mu) are loaded after it so they do
     // not occupy registers while the neighbour links are in flight
     mat3<T> sig;
@@ -174,52 +174,50 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
         site_coords(g, site, c);
         staple_sum<D, T>(Uin, g, site, c, mu, sig);
     }
+    const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
     mat3<T> u;
-    load_link<T>(Uin, (size_t)(mu * 9) * V, V, site, u);
+    load_mat<T>(Uin + ui, u);
     T e[8], el[8], e_old[8];
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        e[a] = Ein[(size_t)(mu * 8 + a) * V + site];
-        el[a] = COMP ? Ein[elo + (size_t)(mu * 8 + a) * V + site] : T(0);
+        e[a] = Ein[ei + a * kTile];
+        el[a] = COMP ? Ein[elo + ei + a * kTile] : T(0);
         e_old[a] = e[a];
     }
     if (MODE & MD_KICK) {
-        mat3<T> m;
-        mul_nn(u, sig, m);
         T f[8];
-        im_tr_generators(m, f);
+        im_tr_generators_of_product(u, sig, f);
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
             if (COMP) {
                 if (k1 != T(0)) comp_add(e[a], el[a], k1 * f[a]);
                 comp_add(e[a], el[a], k2 * f[a]);
-                Eout[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
+                Eout[elo + ei + a * kTile] = el[a];
             } else {
                 if (k1 != T(0)) e[a] = fma(k1, f[a], e[a]);
                 e[a] = fma(k2, f[a], e[a]);
             }
-            Eout[(size_t)(mu * 8 + a) * V + site] = e[a];
+            Eout[ei + a * kTile] = e[a];
         }
     } else if (Eout != Ein) {
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
-            Eout[(size_t)(mu * 8 + a) * V + site] = e[a];
-            if (COMP) Eout[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
+            Eout[ei + a * kTile] = e[a];
+            if (COMP) Eout[elo + ei + a * kTile] = el[a];
         }
     }
     if (MODE & MD_DRIFT) {
-        mat3<T> em, w;
-        adjoint_to_matrix<T>((MODE & MD_DRIFT_OLD_E) ? e_old : e, em);
-        mul_nn(em, u, w);
+        mat3<T> w;
+        adj_mul<T>((MODE & MD_DRIFT_OLD_E) ? e_old : e, u, w);
         if (COMP) {
             mat3<T> ul;
-            load_link<T>(Uin + ulo, (size_t)(mu * 9) * V, V, site, ul);
+            load_mat<T>(Uin + ulo + ui, ul);
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
                 comp_add(u.e[k].re, ul.e[k].re, -drift * w.e[k].im);
                 comp_add(u.e[k].im, ul.e[k].im, drift * w.e[k].re);
             }
-            store_link<T>(Uout + ulo, (size_t)(mu * 9) * V, V, site, ul);
+            store_mat<T>(Uout + ulo + ui, ul);
         } else {
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
@@ -227,7 +225,7 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
                 u.e[k].im = fma(drift, w.e[k].re, u.e[k].im);
             }
         }
-        store_link<T>(Uout, (size_t)(mu * 9) * V, V, site, u);
+        store_mat<T>(Uout + ui, u);
     }
 }
 
@@ -237,12 +235,12 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
 // Im G02, Re G12, Im G12).  Links drift off SU(3) under the first-order link update, so
 // U^dag E U acquires a small trace; keeping the full Hermitian G (not only its su(3)
 // projection) follows the reference, whose G enters the projection step as a matrix.
-template <typename T> __device__ __forceinline__ void herm_load(const T *__restrict__ G, size_t V, uint32_t site,
-                                                                mat3<T> &m) {
-    const T d0 = G[site], d1 = G[V + site], d2 = G[2 * V + site];
-    const T r01 = G[3 * V + site], i01 = G[4 * V + site];
-    const T r02 = G[5 * V + site], i02 = G[6 * V + site];
-    const T r12 = G[7 * V + site], i12 = G[8 * V + site];
+template <typename T> __device__ __forceinline__ void herm_load(const T *__restrict__ G, uint32_t site, mat3<T> &m) {
+    const T *p = G + tix(site, 9, 0);
+    const T d0 = p[0], d1 = p[kTile], d2 = p[2 * kTile];
+    const T r01 = p[3 * kTile], i01 = p[4 * kTile];
+    const T r02 = p[5 * kTile], i02 = p[6 * kTile];
+    const T r12 = p[7 * kTile], i12 = p[8 * kTile];
     m.e[0] = cmk(d0, T(0));
     m.e[4] = cmk(d1, T(0));
     m.e[8] = cmk(d2, T(0));
@@ -253,17 +251,17 @@ template <typename T> __device__ __forceinline__ void herm_load(const T *__restr
     m.e[5] = cmk(r12, i12);
     m.e[7] = cmk(r12, -i12);
 }
-template <typename T> __device__ __forceinline__ void herm_store(T *__restrict__ G, size_t V, uint32_t site,
-                                                                 const mat3<T> &m) {
-    G[site] = m.e[0].re;
-    G[V + site] = m.e[4].re;
-    G[2 * V + site] = m.e[8].re;
-    G[3 * V + site] = m.e[1].re;
-    G[4 * V + site] = m.e[1].im;
-    G[5 * V + site] = m.e[2].re;
-    G[6 * V + site] = m.e[2].im;
-    G[7 * V + site] = m.e[5].re;
-    G[8 * V + site] = m.e[5].im;
+template <typename T> __device__ __forceinline__ void herm_store(T *__restrict__ G, uint32_t site, const mat3<T> &m) {
+    T *p = G + tix(site, 9, 0);
+    p[0] = m.e[0].re;
+    p[kTile] = m.e[4].re;
+    p[2 * kTile] = m.e[8].re;
+    p[3 * kTile] = m.e[1].re;
+    p[4 * kTile] = m.e[1].im;
+    p[5 * kTile] = m.e[2].re;
+    p[6 * kTile] = m.e[2].im;
+    p[7 * kTile] = m.e[5].re;
+    p[8 * kTile] = m.e[5].im;
 }
 
 // G(x) = sum_mu [E_mu(x) - U_mu(x-mu)^dag E_mu(x-mu) U_mu(x-mu)]  (EField::gauss,
@@ -276,7 +274,6 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     double r[1] = {0.0};
     if (site < g.V) {
-        const size_t V = g.V;
         uint32_t c[D];
         site_coords(g, site, c);
         mat3<T> gs;
@@ -284,25 +281,25 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
 #pragma unroll
         for (int mu = 0; mu < D; ++mu) {
             const uint32_t xm = bwd(g, site, c[mu], mu);
+            const size_t ex = tix(site, D * 8, mu * 8), emi = tix(xm, D * 8, mu * 8);
             T ex_c[8], em_c[8];
 #pragma unroll
             for (int a = 0; a < 8; ++a) {
-                ex_c[a] = E[(size_t)(mu * 8 + a) * V + site];
-                em_c[a] = E[(size_t)(mu * 8 + a) * V + xm];
+                ex_c[a] = E[ex + a * kTile];
+                em_c[a] = E[emi + a * kTile];
             }
-            mat3<T> u, ex, em, t, w;
-            load_link<T>(U, (size_t)(mu * 9) * V, V, xm, u);
-            adjoint_to_matrix<T>(ex_c, ex);
-            adjoint_to_matrix<T>(em_c, em);
-            mul_nn(em, u, t);
+            mat3<T> u, ex_m, t, w;
+            load_mat<T>(U + tix(xm, D * 9, mu * 9), u);
+            adjoint_to_matrix<T>(ex_c, ex_m);
+            adj_mul<T>(em_c, u, t);
             mul_an(u, t, w);
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                gs.e[k].re += ex.e[k].re - w.e[k].re;
-                gs.e[k].im += ex.e[k].im - w.e[k].im;
+                gs.e[k].re += ex_m.e[k].re - w.e[k].re;
+                gs.e[k].im += ex_m.e[k].im - w.e[k].im;
             }
         }
-        herm_store(G, V, site, gs);
+        herm_store(G, site, gs);
         T gc[8];
         two_re_tr_generators(gs, gc);
         T s = T(0);
@@ -344,26 +341,26 @@ __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U,
     const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
     const int mu = blockIdx.x % D;
     if (site >= g.V) return;
-    const size_t V = g.V;
-    const size_t elo = (size_t)D * 8 * V;
+    const size_t elo = (size_t)tiles_of(g.V) * D * 8 * kTile;
     uint32_t c[D];
     site_coords(g, site, c);
     mat3<T> u, gx, gp;
-    herm_load(G, V, site, gx);
-    herm_load(G, V, fwd(g, site, c[mu], mu), gp);
-    load_link<T>(U, (size_t)(mu * 9) * V, V, site, u);
+    herm_load(G, site, gx);
+    herm_load(G, fwd(g, site, c[mu], mu), gp);
+    load_mat<T>(U + tix(site, D * 9, mu * 9), u);
+    const size_t ei = tix(site, D * 8, mu * 8);
     T gxc[8], e[8], el[8];
     two_re_tr_generators(gx, gxc);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        e[a] = E[(size_t)(mu * 8 + a) * V + site];
-        el[a] = COMP ? E[elo + (size_t)(mu * 8 + a) * V + site] : T(0);
+        e[a] = E[ei + a * kTile];
+        el[a] = COMP ? E[elo + ei + a * kTile] : T(0);
     }
     projection_step<T, COMP>(u, gx, gxc, gp, e, el);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        E[(size_t)(mu * 8 + a) * V + site] = e[a];
-        if (COMP) E[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
+        E[ei + a * kTile] = e[a];
+        if (COMP) E[elo + ei + a * kTile] = el[a];
     }
 }
 
@@ -381,12 +378,11 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const 
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     double r[1] = {0.0};
     if (site < g.V) {
-        const size_t V = g.V;
-        const size_t elo = (size_t)D * 8 * V;
+        const size_t elo = (size_t)tiles_of(g.V) * D * 8 * kTile;
         uint32_t c[D];
         site_coords(g, site, c);
         mat3<T> gx, gnew;
-        herm_load(Gin, V, site, gx);
+        herm_load(Gin, site, gx);
         T gxc[8];
         two_re_tr_generators(gx, gxc);
         mat_zero(gnew);
@@ -395,18 +391,19 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const 
             T e[8], el[8];
             {
                 mat3<T> u, gp, em;
-                load_link<T>(U, (size_t)(mu * 9) * V, V, site, u);
-                herm_load(Gin, V, fwd(g, site, c[mu], mu), gp);
+                load_mat<T>(U + tix(site, D * 9, mu * 9), u);
+                herm_load(Gin, fwd(g, site, c[mu], mu), gp);
+                const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
                 for (int a = 0; a < 8; ++a) {
-                    e[a] = Ein[(size_t)(mu * 8 + a) * V + site];
-                    el[a] = COMP ? Ein[elo + (size_t)(mu * 8 + a) * V + site] : T(0);
+                    e[a] = Ein[ei + a * kTile];
+                    el[a] = COMP ? Ein[elo + ei + a * kTile] : T(0);
                 }
                 projection_step<T, COMP>(u, gx, gxc, gp, e, el);
 #pragma unroll
                 for (int a = 0; a < 8; ++a) {
-                    Eout[(size_t)(mu * 8 + a) * V + site] = e[a];
-                    if (COMP) Eout[elo + (size_t)(mu * 8 + a) * V + site] = el[a];
+                    Eout[ei + a * kTile] = e[a];
+                    if (COMP) Eout[elo + ei + a * kTile] = el[a];
                 }
                 adjoint_to_matrix<T>(e, em);
 #pragma unroll
@@ -417,19 +414,19 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const 
             }
             {
                 const uint32_t xm = bwd(g, site, c[mu], mu);
-                mat3<T> w, gm, em, t, wm;
-                load_link<T>(U, (size_t)(mu * 9) * V, V, xm, w);
-                herm_load(Gin, V, xm, gm);
+                mat3<T> w, gm, t, wm;
+                load_mat<T>(U + tix(xm, D * 9, mu * 9), w);
+                herm_load(Gin, xm, gm);
                 T gmc[8];
                 two_re_tr_generators(gm, gmc);
+                const size_t ei = tix(xm, D * 8, mu * 8);
 #pragma unroll
                 for (int a = 0; a < 8; ++a) {
-                    e[a] = Ein[(size_t)(mu * 8 + a) * V + xm];
-                    el[a] = COMP ? Ein[elo + (size_t)(mu * 8 + a) * V + xm] : T(0);
+                    e[a] = Ein[ei + a * kTile];
+                    el[a] = COMP ? Ein[elo + ei + a * kTile] : T(0);
                 }
                 projection_step<T, COMP>(w, gm, gmc, gx, e, el);
-                adjoint_to_matrix<T>(e, em);
-                mul_nn(em, w, t);
+                adj_mul<T>(e, w, t);
                 mul_an(w, t, wm);
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
@@ -438,7 +435,7 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const 
                 }
             }
         }
-        herm_store(Gout, V, site, gnew);
+        herm_store(Gout, site, gnew);
         T gc[8];
         two_re_tr_generators(gnew, gc);
         T sum = T(0);
@@ -462,7 +459,6 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     double v[3] = {0.0, 0.0, 0.0};
     if (site < g.V) {
-        const size_t V = g.V;
         uint32_t c[D];
         site_coords(g, site, c);
         T sre = T(0), sim = T(0), sh = T(0);
@@ -472,11 +468,11 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
 #pragma unroll
             for (int nu = mu + 1; nu < D; ++nu) {
                 mat3<T> p, q, A, B;
-                load_link<T>(U, (size_t)(mu * 9) * V, V, site, p);
-                load_link<T>(U, (size_t)(nu * 9) * V, V, xpmu, q);
+                load_mat<T>(U + tix(site, D * 9, mu * 9), p);
+                load_mat<T>(U + tix(xpmu, D * 9, nu * 9), q);
                 mul_nn(p, q, A);
-                load_link<T>(U, (size_t)(nu * 9) * V, V, site, p);
-                load_link<T>(U, (size_t)(mu * 9) * V, V, fwd(g, site, c[nu], nu), q);
+                load_mat<T>(U + tix(site, D * 9, nu * 9), p);
+                load_mat<T>(U + tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), q);
                 mul_nn(p, q, B);
                 T re = T(0), im = T(0);
 #pragma unroll
@@ -511,17 +507,17 @@ __global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (site < g.V) {
-        const size_t V = g.V;
-        const size_t ulo = (size_t)D * 9 * V;
+        const size_t ulo = (size_t)tiles_of(g.V) * D * 9 * kTile;
         uint32_t c[D];
         site_coords(g, site, c);
         auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
-            load_link<T>(Uo, (size_t)(dir * 9) * V, V, x, old_hi);
-            load_link<T>(Un, (size_t)(dir * 9) * V, V, x, new_hi);
+            const size_t i = tix(x, D * 9, dir * 9);
+            load_mat<T>(Uo + i, old_hi);
+            load_mat<T>(Un + i, new_hi);
             if (COMP) {
                 mat3<T> ol, nl;
-                load_link<T>(Uo + ulo, (size_t)(dir * 9) * V, V, x, ol);
-                load_link<T>(Un + ulo, (size_t)(dir * 9) * V, V, x, nl);
+                load_mat<T>(Uo + ulo + i, ol);
+                load_mat<T>(Un + ulo + i, nl);
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
                     diff.e[k].re = (new_hi.e[k].re - old_hi.e[k].re) + (nl.e[k].re - ol.e[k].re);
@@ -625,21 +621,20 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= g.V) return;
-    const size_t V = g.V;
-    const size_t p0 = (size_t)(mu * 9) * V;
-    const size_t ulo = (size_t)D * 9 * V;
+    const size_t p0 = tix(site, D * 9, mu * 9);
+    const size_t ulo = (size_t)tiles_of(g.V) * D * 9 * kTile;
     double r1[3], i1[3], r2[3], i2[3];
 #pragma unroll
     for (int row = 0; row < 3; ++row) {
-        const V2<T> a = U[p0 + (size_t)(row * 3 + 0) * V + site];
-        const V2<T> b = U[p0 + (size_t)(row * 3 + 1) * V + site];
+        const V2<T> a = U[p0 + (row * 3 + 0) * kTile];
+        const V2<T> b = U[p0 + (row * 3 + 1) * kTile];
         r1[row] = a.x;
         i1[row] = a.y;
         r2[row] = b.x;
         i2[row] = b.y;
         if (COMP) {
-            const V2<T> al = U[ulo + p0 + (size_t)(row * 3 + 0) * V + site];
-            const V2<T> bl = U[ulo + p0 + (size_t)(row * 3 + 1) * V + site];
+            const V2<T> al = U[ulo + p0 + (row * 3 + 0) * kTile];
+            const V2<T> bl = U[ulo + p0 + (row * 3 + 1) * kTile];
             r1[row] += al.x;
             i1[row] += al.y;
             r2[row] += bl.x;
@@ -699,8 +694,8 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
             V2<T> h, l;
             split(cols_r[col][row], h.x, l.x);
             split(cols_i[col][row], h.y, l.y);
-            U[p0 + (size_t)(row * 3 + col) * V + site] = h;
-            if (COMP) U[ulo + p0 + (size_t)(row * 3 + col) * V + site] = l;
+            U[p0 + (row * 3 + col) * kTile] = h;
+            if (COMP) U[ulo + p0 + (row * 3 + col) * kTile] = l;
         }
 }
 
@@ -713,7 +708,8 @@ __global__ void __launch_bounds__(128) k_links_from_aos(const double *__restrict
     const int mu = blockIdx.y;
     if (site >= V) return;
     const double *src = aos + ((size_t)site * D + mu) * 18;
-    const size_t ulo = (size_t)D * 9 * V;
+    const size_t ulo = (size_t)tiles_of(V) * D * 9 * kTile;
+    const size_t p0 = tix(site, D * 9, mu * 9);
 #pragma unroll
     for (int col = 0; col < 3; ++col)
 #pragma unroll
@@ -721,7 +717,7 @@ __global__ void __launch_bounds__(128) k_links_from_aos(const double *__restrict
             V2<T> h, l;
             split(src[(col * 3 + row) * 2], h.x, l.x);
             split(src[(col * 3 + row) * 2 + 1], h.y, l.y);
-            const size_t idx = (size_t)(mu * 9 + row * 3 + col) * V + site;
+            const size_t idx = p0 + (row * 3 + col) * kTile;
             U[idx] = h;
             if (COMP) U[ulo + idx] = l;
         }
@@ -733,12 +729,13 @@ __global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ 
     const int mu = blockIdx.y;
     if (site >= V) return;
     double *dst = aos + ((size_t)site * D + mu) * 18;
-    const size_t ulo = (size_t)D * 9 * V;
+    const size_t ulo = (size_t)tiles_of(V) * D * 9 * kTile;
+    const size_t p0 = tix(site, D * 9, mu * 9);
 #pragma unroll
     for (int col = 0; col < 3; ++col)
 #pragma unroll
         for (int row = 0; row < 3; ++row) {
-            const size_t idx = (size_t)(mu * 9 + row * 3 + col) * V + site;
+            const size_t idx = p0 + (row * 3 + col) * kTile;
             const V2<T> v = U[idx];
             double re = (double)v.x, im = (double)v.y;
             if (COMP) {
@@ -757,13 +754,14 @@ __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restric
     const int mu = blockIdx.y;
     if (site >= V) return;
     const double *src = aos + ((size_t)site * D + mu) * 8;
-    const size_t elo = (size_t)D * 8 * V;
+    const size_t elo = (size_t)tiles_of(V) * D * 8 * kTile;
+    const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
         T h, l;
         split(src[a], h, l);
-        E[(size_t)(mu * 8 + a) * V + site] = h;
-        if (COMP) E[elo + (size_t)(mu * 8 + a) * V + site] = l;
+        E[ei + a * kTile] = h;
+        if (COMP) E[elo + ei + a * kTile] = l;
     }
 }
 template <int D, typename T, bool COMP>
@@ -773,11 +771,12 @@ __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, 
     const int mu = blockIdx.y;
     if (site >= V) return;
     double *dst = aos + ((size_t)site * D + mu) * 8;
-    const size_t elo = (size_t)D * 8 * V;
+    const size_t elo = (size_t)tiles_of(V) * D * 8 * kTile;
+    const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        double x = (double)E[(size_t)(mu * 8 + a) * V + site];
-        if (COMP) x += (double)E[elo + (size_t)(mu * 8 + a) * V + site];
+        double x = (double)E[ei + a * kTile];
+        if (COMP) x += (double)E[elo + ei + a * kTile];
         dst[a] = x;
     }
 }
@@ -787,23 +786,26 @@ __global__ void __launch_bounds__(256) k_gauss_to_aos(const T *__restrict__ G, d
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     if (site >= V) return;
     mat3<T> m;
-    herm_load(G, (size_t)V, site, m);
+    herm_load(G, site, m);
     T gc[8];
     two_re_tr_generators(m, gc);
 #pragma unroll
     for (int a = 0; a < 8; ++a) out[(size_t)site * 8 + a] = (double)gc[a];
 }
 
-// identity links (hi planes; lo planes, when present, are cleared by the caller)
-template <typename T>
-__global__ void __launch_bounds__(256) k_links_identity(V2<T> *__restrict__ U, size_t V, int D) {
-    const size_t n = V * 9 * D;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int k = (int)((i / V) % 9);
+// identity links (hi array; the lo array, when present, is cleared by the caller)
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_links_identity(V2<T> *__restrict__ U, uint32_t V) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    const size_t p0 = tix(site, D * 9, mu * 9);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
         V2<T> v;
         v.x = (k == 0 || k == 4 || k == 8) ? T(1) : T(0);
         v.y = T(0);
-        U[i] = v;
+        U[p0 + k * kTile] = v;
     }
 }
 
@@ -880,11 +882,12 @@ __global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32
             z[4 * j + 3] = (T)d2;
         }
     }
-    const size_t elo = (size_t)D * 8 * V;
+    const size_t elo = (size_t)tiles_of(V) * D * 8 * kTile;
+    const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        E[(size_t)(mu * 8 + a) * V + site] = z[a] * sd;
-        if (COMP) E[elo + (size_t)(mu * 8 + a) * V + site] = T(0);
+        E[ei + a * kTile] = z[a] * sd;
+        if (COMP) E[elo + ei + a * kTile] = T(0);
     }
 }
 
@@ -930,8 +933,8 @@ __global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uin
         }
         if (hypot(dr, di) > eps) break;
     }
-    const size_t p0 = (size_t)(mu * 9) * V;
-    const size_t ulo = (size_t)D * 9 * V;
+    const size_t p0 = tix(site, D * 9, mu * 9);
+    const size_t ulo = (size_t)tiles_of(V) * D * 9 * kTile;
 #pragma unroll
     for (int row = 0; row < 3; ++row) {
         V2<T> a, b, al, bl;
@@ -939,11 +942,11 @@ __global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uin
         split(i1[row], a.y, al.y);
         split(r2[row], b.x, bl.x);
         split(i2[row], b.y, bl.y);
-        U[p0 + (size_t)(row * 3 + 0) * V + site] = a;
-        U[p0 + (size_t)(row * 3 + 1) * V + site] = b;
+        U[p0 + (row * 3 + 0) * kTile] = a;
+        U[p0 + (row * 3 + 1) * kTile] = b;
         if (COMP) {
-            U[ulo + p0 + (size_t)(row * 3 + 0) * V + site] = al;
-            U[ulo + p0 + (size_t)(row * 3 + 1) * V + site] = bl;
+            U[ulo + p0 + (row * 3 + 0) * kTile] = al;
+            U[ulo + p0 + (row * 3 + 1) * kTile] = bl;
         }
     }
 }

@@ -308,7 +308,13 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaMallocHost", __LINE__);
     }
     if (!rc) {
-        cudaError_t e = s->ops->links_cold(*s, s->U[0]);
+        // every buffer starts zeroed: the padding of the last tile stays zero for the sums
+        cudaError_t e = cudaSuccess;
+        for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaMemsetAsync(s->U[i], 0, s->link_bytes(), s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->E_alt, 0, s->efield_bytes(), s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->G, 0, s->gauss_bytes(), s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->G_alt, 0, s->gauss_bytes(), s->stream);
+        if (e == cudaSuccess) e = s->ops->links_cold(*s, s->U[0]);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->E, 0, s->efield_bytes(), s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "state initialisation", __LINE__);

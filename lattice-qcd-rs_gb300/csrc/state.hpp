@@ -62,11 +62,13 @@ struct State {
     const Ops *ops = nullptr;
     Prof *prof = nullptr; // non-null while profiling is enabled
 
-    size_t link_elems() const { return (size_t)V * dim * 9; }   // complex elements
+    // arrays are stored in tiles of 32 sites (padded; see tix() in su3.cuh)
+    size_t padded_sites() const { return ((size_t)V + 31) / 32 * 32; }
+    size_t link_elems() const { return padded_sites() * dim * 9; }   // complex elements
     size_t link_bytes() const { return link_elems() * 2 * real_bytes * (comp ? 2 : 1); }
-    size_t efield_elems() const { return (size_t)V * dim * 8; } // reals (hi part)
+    size_t efield_elems() const { return padded_sites() * dim * 8; } // reals (hi part)
     size_t efield_bytes() const { return efield_elems() * real_bytes * (comp ? 2 : 1); }
-    size_t gauss_bytes() const { return (size_t)V * 9 * real_bytes; }
+    size_t gauss_bytes() const { return padded_sites() * 9 * real_bytes; }
 };
 
 // Device operations of one (D, T, COMP) instantiation.  Launches are asynchronous on

@@ -192,6 +192,26 @@ int lq_profile_enable(lq_state *s, int on);
 /* launches and total milliseconds of one class since the last reset; also resets when reset != 0 */
 int lq_profile_read(lq_state *s, int kernel_class, long long *launches, double *total_ms, int reset);
 
+/* ---------------------------------------------------------------- without allocation
+ * No counterpart in the reference.  For callers that cannot let this library allocate device
+ * memory -- code running inside a CUDA-graph capture (cudaMalloc cannot be captured), code
+ * whose device memory belongs to one pool or arena (an embedding framework, a memory-capped
+ * MPS client), and loops that cannot afford the device-wide synchronisation of cudaMalloc /
+ * cudaFree.  Computes the plaquette sums of links the caller holds on the device in the serde
+ * layout (double[L^dim * dim][18]) and writes them to d_out[0..2] on the device:
+ *   d_out[0] = sum (1 - Re Tr P / 3)   (hamiltonian_links = beta * d_out[0])
+ *   d_out[1] = sum Re Tr P, d_out[2] = sum Im Tr P
+ *              (average_trace_plaquette = (d_out[1] + i d_out[2]) / (L^dim * dim (dim-1) / 2)).
+ * The work is enqueued on `stream` (a cudaStream_t; NULL = legacy default stream) and the call
+ * returns without synchronising.  Limit: L^dim <= 8,388,608 sites; a larger lattice returns
+ * LQ_ERR_INVALID_ARGUMENT with the reason in lq_last_error_string.  Its scratch is one fixed
+ * 1.5 MiB device array that every device loading the library holds until the process exits;
+ * all calls share it, so calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  The first call on a device looks up the
+ * array's device address with that device current; make that first call before any stream
+ * capture. */
+int lq_plaquette_sums_noalloc(int dim, int L, const double *d_links, double *d_out, void *stream);
+
 /* ---------------------------------------------------------------- diagnostics */
 const char *lq_status_string(int status);
 /* Text of the last error on this host thread (CUDA error name and call site). */

@@ -226,6 +226,11 @@ bool valid_std_dev(double sd) { return sd >= 0.0 && !std::isinf(sd); }
 
 } // namespace
 
+namespace lq {
+// lets other translation units of the library report an error through lq_last_error_string
+void set_last_error(const char *text) { g_last_error = text; }
+} // namespace lq
+
 extern "C" {
 
 int lq_version(void) { return 100; }

@@ -70,6 +70,7 @@ SIGNATURES = {
     "lq_hmc_propose": (_i32, [_vp, _f64, _i32, _dp, _dp, _dp]),
     "lq_hmc_decide": (_i32, [_vp, _i32]),
     "lq_hmc_trajectory": (_i32, [_vp, _f64, _i32, _u64, _u64, _f64, _i32, _ip, _dp, _dp, _ip]),
+    "lq_plaquette_sums_noalloc": (_i32, [_i32, _i32, _vp, _vp, _vp]),
     "lq_profile_enable": (_i32, [_vp, _i32]),
     "lq_profile_read": (_i32, [_vp, _i32, _llp, _dp, _i32]),
     "lq_status_string": (ctypes.c_char_p, [_i32]),

@@ -20,7 +20,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
 ]
-SOURCES = ["lq_api.cu", "lq_f64.cu", "lq_f32.cu", "lq_mixed.cu"]
+SOURCES = ["lq_api.cu", "lq_f64.cu", "lq_f32.cu", "lq_mixed.cu", "lq_noalloc.cu"]
 
 
 def nvcc():

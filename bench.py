@@ -202,6 +202,12 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+# DRAM bytes (read + write) per link of one k_md kick+drift launch, from one ncu capture at 28^4
+# (profiles/k_md_mixed_28x4.md: 994.1 MB for 2,458,624 links); traffic scales with the links of
+# a launch, so the full-size value is this times the links.
+NCU_MD_TRAFFIC_PER_LINK = {"mixed": 994.1e6 / 2458624}
+
+
 def algorithmic_md_bytes(n_links, md_steps, real_bytes):
     """Bytes moved by the fused MD kernels of one trajectory at ideal neighbour reuse.
     kick+drift launch: read U (18 reals) + E (8) + write E (8) + U' (18) = 52 reals per link;
@@ -409,7 +415,10 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (links %.0f MB)" % (n_links * 18 * real_bytes / 1e6)},
             "roofline": {"bound": "hbm", "kernel": "k_md (fused force + kick + drift)", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": None, "algorithmic_bytes_per_link": 52 * real_bytes,
+                         "traffic": (NCU_MD_TRAFFIC_PER_LINK[args.precision] * n_links
+                                     if args.precision in NCU_MD_TRAFFIC_PER_LINK else None),
+                         "traffic_source": "ncu dram bytes per link at 28^4 scaled to 32^4",
+                         "algorithmic_bytes_per_link": 52 * real_bytes,
                          "md_launch_ms": md_ms / max(1, md_launches)},
             "kernel_ms": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
             "gpu_launches": launches,

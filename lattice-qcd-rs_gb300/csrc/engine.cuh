@@ -91,10 +91,13 @@ template <int D, typename T, bool COMP> struct Engine {
         *n_partials = blocks;
         return cudaGetLastError();
     }
+    // The projection runs on the hi parts only, also for compensated storage: the projected
+    // field is the start momentum of a trajectory, whose low-order bits do not enter Delta H
+    // (both Hamiltonians see the same start); the caller clears the lo parts afterwards.
     static cudaError_t gauss_sweep(State &s, const void *U, uint32_t *n_partials) {
         const uint32_t blocks = (s.V + 127) / 128;
-        k_gauss_sweep<D, T, COMP><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.E_alt,
-                                                                 (const T *)s.G, (T *)s.G_alt, geo(s), s.partial);
+        k_gauss_sweep<D, T, false><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.E_alt,
+                                                                  (const T *)s.G, (T *)s.G_alt, geo(s), s.partial);
         *n_partials = blocks;
         return cudaGetLastError();
     }

@@ -190,8 +190,9 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
             if (COMP) {
-                if (k1 != T(0)) comp_add(e[a], el[a], k1 * f[a]);
-                comp_add(e[a], el[a], k2 * f[a]);
+                // compensated storage: one exact-sum update with both half-kicks (the separate
+                // adds of the FP64 form only reproduce the reference's FP64 rounding)
+                comp_add(e[a], el[a], (k1 + k2) * f[a]);
                 Eout[elo + ei + a * kTile] = el[a];
             } else {
                 if (k1 != T(0)) e[a] = fma(k1, f[a], e[a]);
@@ -553,28 +554,35 @@ __global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict
             return s;
         };
         T acc = T(0);
-#pragma unroll
+#pragma unroll 1
         for (int mu = 0; mu < D; ++mu) {
             const uint32_t xpmu = fwd(g, site, c[mu], mu);
-#pragma unroll
+#pragma unroll 1
             for (int nu = mu + 1; nu < D; ++nu) {
                 const uint32_t xpnu = fwd(g, site, c[nu], nu);
-                mat3<T> A, An, dA, B, Bn, dB, C, Cn, dC, Dd, Dn, dD, q1, s1, l1, t;
-                load_pair(mu, site, A, An, dA);
-                load_pair(nu, xpmu, B, Bn, dB);
-                load_pair(mu, xpnu, C, Cn, dC);
-                load_pair(nu, site, Dd, Dn, dD);
+                // links: A = U_mu(x), B = U_nu(x+mu), C = U_mu(x+nu), Dd = U_nu(x); primes: new.
+                // Evaluated in an order that keeps about four matrices live.
+                mat3<T> q1, t, s1, x_old, x_new, dx, l1;
                 T term = T(0);
-                mul_nn(Dn, Cn, q1);       // Q1 = Dd' C'       (C'^dag Dd'^dag = Q1^dag)
-                mul_na(Bn, q1, s1);       // B' C'^dag Dd'^dag
-                term += re_tr_nn(dA, s1); // Tr(dA B' C'^dag Dd'^dag)
-                mul_an(q1, A, t);         // C'^dag Dd'^dag A
-                term += re_tr_nn(dB, t);  // Tr(A dB C'^dag Dd'^dag)
-                mul_nn(A, B, l1);         // L1 = A B
-                mul_an(Dn, l1, t);        // Dd'^dag A B
-                term += re_tr_na(t, dC);  // Tr(A B dC^dag Dd'^dag) = Re Tr((Dd'^dag A B) dC^dag)
-                mul_na(l1, C, t);         // A B C^dag
-                term += re_tr_na(t, dD);  // Tr(A B C^dag dDd^dag)
+                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
+                load_mat<T>(Un + tix(xpnu, D * 9, mu * 9), t);     // C'
+                mul_nn(x_new, t, q1);                                  // Q1 = Dd' C'
+                load_mat<T>(Un + tix(xpmu, D * 9, nu * 9), t);     // B'
+                mul_na(t, q1, s1);                                     // B' C'^dag Dd'^dag
+                load_pair(mu, site, x_old, x_new, dx);                 // A, A', dA
+                term += re_tr_nn(dx, s1);                              // Tr(dA B' C'^dag Dd'^dag)
+                mul_an(q1, x_old, t);                                  // C'^dag Dd'^dag A
+                mat3<T> a_old = x_old;
+                load_pair(nu, xpmu, x_old, x_new, dx);                 // B, B', dB
+                term += re_tr_nn(dx, t);                               // Tr(A dB C'^dag Dd'^dag)
+                mul_nn(a_old, x_old, l1);                              // L1 = A B
+                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
+                mul_an(x_new, l1, t);                                  // Dd'^dag A B
+                load_pair(mu, xpnu, x_old, x_new, dx);                 // C, C', dC
+                term += re_tr_na(t, dx);                               // Tr(A B dC^dag Dd'^dag)
+                mul_na(l1, x_old, t);                                  // A B C^dag
+                load_pair(nu, site, x_old, x_new, dx);                 // Dd, Dd', dDd
+                term += re_tr_na(t, dx);                               // Tr(A B C^dag dDd^dag)
                 acc += term;
             }
         }

@@ -218,6 +218,11 @@ int project_gauss(State &s, int max_steps, int *steps_done) {
             return LQ_ERR_NOT_CONVERGED;
         }
     }
+    if (fused && s.comp) {
+        // the sweeps updated the hi parts only: the projected field is hi + 0
+        const size_t half = s.efield_bytes() / 2;
+        LQ_CK(cudaMemsetAsync((char *)s.E + half, 0, half, s.stream));
+    }
     if (steps_done) *steps_done = steps;
     return LQ_OK;
 }

@@ -72,7 +72,20 @@ enum lq_integration_mode {
     LQ_SYNC_LEAP = 1,   /* integrate_sync_leap:  E += dt/2 F(U)                       (state becomes leap-frog) */
     LQ_LEAP_LEAP = 2,   /* integrate_leap_leap:  U += dt dU(E,U);  E += dt F(U')      */
     LQ_LEAP_SYNC = 3,   /* integrate_leap_sync:  U += dt dU(E,U);  E += dt/2 F(U')    (state becomes synchronous) */
-    LQ_SYMPLECTIC = 4   /* integrate_symplectic: E += dt/2 F(U); U += dt dU(E,U); E += dt/2 F(U') */
+    LQ_SYMPLECTIC = 4,  /* integrate_symplectic: E += dt/2 F(U); U += dt dU(E,U); E += dt/2 F(U') */
+    /* no counterpart in the reference's integrators: the symplectic step with the link moved on the
+     * group, U' = exp(i dt sqrt(2 C_A)/size E) U, the exponential by the Cayley-Hamilton recursion
+     * of su3::su3_exp_i (src/su3.rs:832-855); _REUNITARIZE applies normalize_link_matrices
+     * (src/su3.rs:290-309) to every link after each step, in the same kernel */
+    LQ_SYMPLECTIC_EXP = 5,
+    LQ_SYMPLECTIC_EXP_REUNITARIZE = 6
+};
+
+/* link update used by lq_hmc_propose / lq_hmc_trajectory (lq_state_set_link_update) */
+enum lq_link_update {
+    LQ_LINK_UPDATE_EULER = 0,            /* integrate_link, the reference's first-order update (default) */
+    LQ_LINK_UPDATE_EXP = 1,              /* exp(i dt c E) U */
+    LQ_LINK_UPDATE_EXP_REUNITARIZE = 2   /* exp(i dt c E) U, then orthonormalize_matrix per step */
 };
 
 typedef struct lq_state lq_state;
@@ -95,6 +108,8 @@ int lq_state_set_stream(lq_state *s, void *cuda_stream);
 int lq_state_info(const lq_state *s, int *dim, int *L, double *size, double *beta, int *precision,
                   long long *n_sites, long long *t, int *is_leap);
 int lq_state_set_beta(lq_state *s, double beta);
+/* choose the link update of the HMC proposal (lq_link_update); Euler, the reference's, by default */
+int lq_state_set_link_update(lq_state *s, int link_update);
 /* Device bytes held by the state (links buffers, E, Gauss buffer, staging). */
 int lq_state_device_bytes(const lq_state *s, size_t *bytes);
 
@@ -151,10 +166,25 @@ int lq_normalize_link_matrices(lq_state *s);
  * n == 0 gives LQ_ERR_ZERO_INTEGRATION.  SYNC_LEAP requires a synchronous state and leaves a
  * leap-frog state; LEAP_LEAP requires leap-frog; LEAP_SYNC requires leap-frog and leaves a
  * synchronous state; SYNC_SYNC / SYMPLECTIC require a synchronous state (else
- * LQ_ERR_WRONG_STATE_KIND).  t advances as in the reference (sync_leap does not advance it). */
+ * LQ_ERR_WRONG_STATE_KIND).  t advances as in the reference (sync_leap does not advance it).
+ * LQ_SYMPLECTIC_EXP(_REUNITARIZE) behave as LQ_SYMPLECTIC with the exponential link update. */
 int lq_integrate(lq_state *s, int mode, double dt, int n);
 /* simulate_using_leapfrog_n (src/simulation/state.rs:318-357) */
 int lq_leapfrog_n(lq_state *s, double dt, int n);
+
+/* ---------------------------------------------------------------- differentiation
+ * The gauge force is the adjoint of the Wilson action: a forward / backward pair in the shape of
+ * an autograd function.  No reference counterpart as an API; the reference's force is
+ * derivative_e (src/simulation/state.rs:1420-1448), which equals -sqrt(2 C_A)/(size beta) times
+ * the backward below. */
+/* forward: S = beta sum_x sum_{mu<nu} (1 - Re Tr P / 3), the same value as lq_hamiltonian_links */
+int lq_wilson_action(lq_state *s, double *out);
+/* backward: dS/dtheta^a for U_mu(x) -> exp(i theta^a T^a) U_mu(x), every link,
+ * out: double[V][D][8] (the E-field layout) = beta/3 Im Tr(T^a U_mu(x) Sigma_mu(x)) */
+int lq_wilson_action_backward(lq_state *s, double *grad, size_t n_doubles);
+/* U_link <- exp(i angle T^a) U_link for one link (link = site*D + mu, a = generator 0..7), for
+ * finite-difference probes of the action */
+int lq_link_rotate(lq_state *s, long long link, int generator, double angle);
 
 /* ---------------------------------------------------------------- HMC
  * HybridMonteCarloDiagnostic::next_element (src/simulation/monte_carlo/hybrid_monte_carlo.rs:465-471,

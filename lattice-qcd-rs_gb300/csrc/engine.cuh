@@ -48,8 +48,19 @@ template <int D, typename T, bool COMP> struct Engine {
         k_efield_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V);
         return cudaGetLastError();
     }
-    static cudaError_t efield_to_aos(State &s, double *d_aos) {
-        k_efield_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)s.E, d_aos, s.V);
+    static cudaError_t efield_to_aos(State &s, const void *E, double *d_aos) {
+        k_efield_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)E, d_aos, s.V);
+        return cudaGetLastError();
+    }
+    // out <- scale * Im Tr(T^a U_mu(x) Sigma_mu(x)) on every link (out zeroed by the caller)
+    static cudaError_t force(State &s, const void *U, void *out, double scale) {
+        const dim3 grid(((s.V + 127) / 128) * D, 1, 1);
+        k_md<D, T, COMP, MD_KICK><<<grid, 128, 0, s.stream>>>((const V2<T> *)U, (V2<T> *)U, (const T *)out, (T *)out,
+                                                               geo(s), T(0), (T)scale, T(0));
+        return cudaGetLastError();
+    }
+    static cudaError_t link_rotate(State &s, void *U, uint32_t site, int mu, int a, double angle) {
+        k_link_rotate<D, T, COMP><<<1, 32, 0, s.stream>>>((V2<T> *)U, s.V, site, mu, a, (T)angle);
         return cudaGetLastError();
     }
     static cudaError_t efield_normal(State &s, uint64_t seed, uint64_t counter, double sd) {
@@ -71,18 +82,22 @@ template <int D, typename T, bool COMP> struct Engine {
         V2<T> *out = (V2<T> *)Uout;
         const T *ei = (const T *)Ein;
         T *eo = (T *)Eout;
+#define LQ_MD_CASE(M)                                                                                                  \
+    case (M): k_md<D, T, COMP, (M)><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
         switch (mode) {
-        case MD_KICK: k_md<D, T, COMP, MD_KICK><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
-        case MD_DRIFT: k_md<D, T, COMP, MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
-        case MD_KICK | MD_DRIFT:
-            k_md<D, T, COMP, MD_KICK | MD_DRIFT><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift);
-            break;
-        case MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E:
-            k_md<D, T, COMP, MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E>
-                <<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift);
-            break;
+            LQ_MD_CASE(MD_KICK)
+            LQ_MD_CASE(MD_DRIFT)
+            LQ_MD_CASE(MD_KICK | MD_DRIFT)
+            LQ_MD_CASE(MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E)
+            LQ_MD_CASE(MD_DRIFT | MD_EXP)
+            LQ_MD_CASE(MD_KICK | MD_DRIFT | MD_EXP)
+            LQ_MD_CASE(MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E | MD_EXP)
+            LQ_MD_CASE(MD_DRIFT | MD_EXP | MD_REUNIT)
+            LQ_MD_CASE(MD_KICK | MD_DRIFT | MD_EXP | MD_REUNIT)
+            LQ_MD_CASE(MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E | MD_EXP | MD_REUNIT)
         default: return cudaErrorInvalidValue;
         }
+#undef LQ_MD_CASE
         return cudaGetLastError();
     }
     static cudaError_t gauss(State &s, const void *U, uint32_t *n_partials) {
@@ -153,7 +168,7 @@ template <int D, typename T, bool COMP> struct Engine {
         static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
                                 efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
                                 gauss_step,     gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
-                                normalize,      finalize};
+                                normalize,      finalize,       force,         link_rotate};
         return &ops;
     }
 };

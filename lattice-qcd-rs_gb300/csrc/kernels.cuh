@@ -144,7 +144,7 @@ __device__ __forceinline__ void staple_sum(const V2<T> *__restrict__ U, const Ge
     }
 }
 
-enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4 };
+enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4, MD_EXP = 8, MD_REUNIT = 16 };
 
 // One thread per link.  Blocks are ordered with mu fastest (blockIdx.x = site_block*D + mu)
 // so the D directions of a block of sites run together and the neighbour links they share
@@ -158,6 +158,9 @@ enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4 };
 //         (derivative_u + integrate_link, src/simulation/state.rs:1407-1417,
 //          src/integrator/mod.rs:216-233), with E after the kick or, with DRIFT_OLD_E,
 //         before it (integrate_sync_sync integrates both fields from the old state).
+//         With EXP the link moves on the group instead: U' = exp(i drift E) U, the
+//         exponential by su3_exp_i's Cayley-Hamilton recursion; REUNIT then applies
+//         orthonormalize_matrix to the result (in double, from hi + lo).
 template <int D, typename T, bool COMP, int MODE>
 __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout,
                                   Geo<D> g, T k1, T k2, T drift) {
@@ -208,26 +211,80 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
         }
     }
     if (MODE & MD_DRIFT) {
+        const T *ed = (MODE & MD_DRIFT_OLD_E) ? e_old : e;
+        // w: the increment U' - U
         mat3<T> w;
-        adj_mul<T>((MODE & MD_DRIFT_OLD_E) ? e_old : e, u, w);
-        if (COMP) {
-            mat3<T> ul;
-            load_mat<T>(Uin + ulo + ui, ul);
+        if (MODE & MD_EXP) {
+            T v[8];
 #pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                comp_add(u.e[k].re, ul.e[k].re, -drift * w.e[k].im);
-                comp_add(u.e[k].im, ul.e[k].im, drift * w.e[k].re);
-            }
-            store_mat<T>(Uout + ulo + ui, ul);
+            for (int a = 0; a < 8; ++a) v[a] = drift * ed[a];
+            mat3<T> r;
+            su3_exp_i_minus_one<T>(v, r);
+            mul_nn(r, u, w);
         } else {
+            mat3<T> x;
+            adj_mul<T>(ed, u, x);
 #pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                u.e[k].re = fma(-drift, w.e[k].im, u.e[k].re);
-                u.e[k].im = fma(drift, w.e[k].re, u.e[k].im);
+            for (int k = 0; k < 9; ++k) w.e[k] = cmk(-drift * x.e[k].im, drift * x.e[k].re);
+        }
+        mat3<T> ul;
+        if (COMP) load_mat<T>(Uin + ulo + ui, ul);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            if (COMP) {
+                comp_add(u.e[k].re, ul.e[k].re, w.e[k].re);
+                comp_add(u.e[k].im, ul.e[k].im, w.e[k].im);
+            } else {
+                u.e[k].re += w.e[k].re;
+                u.e[k].im += w.e[k].im;
             }
         }
+        if (MODE & MD_REUNIT) {
+            double re[9], im[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                re[k] = (double)u.e[k].re + (COMP ? (double)ul.e[k].re : 0.0);
+                im[k] = (double)u.e[k].im + (COMP ? (double)ul.e[k].im : 0.0);
+            }
+            orthonormalize_d(re, im);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                T lr, li;
+                split(re[k], u.e[k].re, lr);
+                split(im[k], u.e[k].im, li);
+                if (COMP) ul.e[k] = cmk(lr, li);
+            }
+        }
+        if (COMP) store_mat<T>(Uout + ulo + ui, ul);
         store_mat<T>(Uout + ui, u);
     }
+}
+
+// U <- exp(i angle T^a) U for one link (finite-difference probes of the action)
+template <int D, typename T, bool COMP>
+__global__ void k_link_rotate(V2<T> *__restrict__ U, uint32_t V, uint32_t site, int mu, int a, T angle) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const size_t ui = tix(site, D * 9, mu * 9), ulo = (size_t)tiles_of(V) * D * 9 * kTile;
+    T v[8];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) v[b] = (b == a) ? angle : T(0);
+    mat3<T> u, ul, r, w;
+    load_mat<T>(U + ui, u);
+    if (COMP) load_mat<T>(U + ulo + ui, ul);
+    su3_exp_i_minus_one<T>(v, r);
+    mul_nn(r, u, w);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        if (COMP) {
+            comp_add(u.e[k].re, ul.e[k].re, w.e[k].re);
+            comp_add(u.e[k].im, ul.e[k].im, w.e[k].im);
+        } else {
+            u.e[k].re += w.e[k].re;
+            u.e[k].im += w.e[k].im;
+        }
+    }
+    store_mat<T>(U + ui, u);
+    if (COMP) store_mat<T>(U + ulo + ui, ul);
 }
 
 // ------------------------------------------------------------------ Gauss law

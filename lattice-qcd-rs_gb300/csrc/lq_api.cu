@@ -163,11 +163,19 @@ int fetch_out(State &s, int count) {
 // E <- E + dt/2 F(U_k) (+ dt/2 F(U_k) of the next step) ...; U_{k+1} = U_k + dt dU(E, U_k).
 // With e_to_alt the first kick reads s.E and writes s.E_alt (later steps update s.E_alt in
 // place), so the start momenta survive in s.E.
-int run_symplectic(State &s, int src, double dt, int n, bool e_to_alt, int *final_buf) {
+int link_update_bits(int link_update) {
+    switch (link_update) {
+    case LQ_LINK_UPDATE_EXP: return lq::MD_EXP;
+    case LQ_LINK_UPDATE_EXP_REUNITARIZE: return lq::MD_EXP | lq::MD_REUNIT;
+    default: return 0;
+    }
+}
+
+int run_symplectic(State &s, int src, double dt, int n, bool e_to_alt, int link_update, int *final_buf) {
     const int a = other_buffer(s, src, -1);
     const int b = other_buffer(s, src, a);
     void *ew = e_to_alt ? s.E_alt : s.E;
-    const int KD = lq::MD_KICK | lq::MD_DRIFT;
+    const int KD = lq::MD_KICK | lq::MD_DRIFT | link_update_bits(link_update);
     LQ_LAUNCH(s, LQ_KERNEL_MD, s.ops->md(s, s.U[src], s.U[a], s.E, ew, KD, 0.0, dt / 2.0, dt));
     int cur = a, nxt = b;
     for (int i = 1; i < n; ++i) {
@@ -395,6 +403,15 @@ int lq_state_set_beta(lq_state *s, double beta) {
     return LQ_OK;
 }
 
+int lq_state_set_link_update(lq_state *s, int link_update) {
+    LQ_CHECK_STATE(s);
+    if (link_update < LQ_LINK_UPDATE_EULER || link_update > LQ_LINK_UPDATE_EXP_REUNITARIZE)
+        return LQ_ERR_INVALID_ARGUMENT;
+    s->link_update = link_update;
+    s->has_pending = 0;
+    return LQ_OK;
+}
+
 int lq_state_device_bytes(const lq_state *s, size_t *bytes) {
     LQ_CHECK_STATE(s);
     if (!bytes) return LQ_ERR_INVALID_ARGUMENT;
@@ -468,7 +485,7 @@ int lq_efield_download(lq_state *s, double *efield, size_t n) {
     const size_t bytes = n * sizeof(double);
     int rc = ensure_staging(*s, bytes);
     if (rc) return rc;
-    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_to_aos(*s, (double *)s->staging));
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_to_aos(*s, s->E, (double *)s->staging));
     LQ_CK(cudaMemcpyAsync(efield, s->staging, bytes, cudaMemcpyDeviceToHost, s->stream));
     LQ_CK(sync_stream(*s));
     return LQ_OK;
@@ -567,6 +584,38 @@ int lq_gauss_download(lq_state *s, double *out, size_t n_doubles) {
     return LQ_OK;
 }
 
+// ------------------------------------------------------------------ differentiation
+int lq_wilson_action(lq_state *s, double *out) { return lq_hamiltonian_links(s, out); }
+
+int lq_wilson_action_backward(lq_state *s, double *grad, size_t n) {
+    LQ_CHECK_STATE(s);
+    if (!grad) return LQ_ERR_INVALID_ARGUMENT;
+    if (n != (size_t)s->V * s->dim * 8) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n * sizeof(double);
+    int rc = ensure_staging(*s, bytes);
+    if (rc) return rc;
+    s->has_pending = 0;
+    // dS/dtheta^a = beta/3 Im Tr(T^a U Sigma): S = beta sum (1 - Re Tr P / 3) and
+    // d/dtheta Re Tr(exp(i theta T) U Sigma) = -Im Tr(T U Sigma) at theta = 0
+    LQ_CK(cudaMemsetAsync(s->E_alt, 0, s->efield_bytes(), s->stream));
+    LQ_LAUNCH(*s, LQ_KERNEL_MD, s->ops->force(*s, s->U[s->cur], s->E_alt, s->beta / 3.0));
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_to_aos(*s, s->E_alt, (double *)s->staging));
+    LQ_CK(cudaMemcpyAsync(grad, s->staging, bytes, cudaMemcpyDeviceToHost, s->stream));
+    LQ_CK(sync_stream(*s));
+    return LQ_OK;
+}
+
+int lq_link_rotate(lq_state *s, long long link, int generator, double angle) {
+    LQ_CHECK_STATE(s);
+    if (link < 0 || link >= (long long)s->V * s->dim || generator < 0 || generator > 7) return LQ_ERR_INVALID_ARGUMENT;
+    const uint32_t site = (uint32_t)(link / s->dim);
+    const int mu = (int)(link % s->dim);
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->link_rotate(*s, s->U[s->cur], site, mu, generator, angle));
+    LQ_CK(sync_stream(*s));
+    state_changed(*s);
+    return LQ_OK;
+}
+
 // ------------------------------------------------------------------ updates
 int lq_project_gauss(lq_state *s, int max_steps, int *steps_done) {
     LQ_CHECK_STATE(s);
@@ -584,7 +633,7 @@ int lq_normalize_link_matrices(lq_state *s) {
 
 int lq_integrate(lq_state *s, int mode, double dt, int n) {
     LQ_CHECK_STATE(s);
-    if (mode < LQ_SYNC_SYNC || mode > LQ_SYMPLECTIC) return LQ_ERR_INVALID_ARGUMENT;
+    if (mode < LQ_SYNC_SYNC || mode > LQ_SYMPLECTIC_EXP_REUNITARIZE) return LQ_ERR_INVALID_ARGUMENT;
     if (n <= 0) return LQ_ERR_ZERO_INTEGRATION;
     const bool needs_leap = (mode == LQ_LEAP_LEAP || mode == LQ_LEAP_SYNC);
     if ((needs_leap && !s->leap) || (!needs_leap && s->leap)) return LQ_ERR_WRONG_STATE_KIND;
@@ -627,9 +676,12 @@ int lq_integrate(lq_state *s, int mode, double dt, int n) {
         st.leap = 0;
         st.t += 1;
         break;
-    default: { // LQ_SYMPLECTIC
+    default: { // LQ_SYMPLECTIC, LQ_SYMPLECTIC_EXP, LQ_SYMPLECTIC_EXP_REUNITARIZE
         int fin = -1;
-        int rc = run_symplectic(st, st.cur, dt, n, false, &fin);
+        const int lu = mode == LQ_SYMPLECTIC_EXP ? LQ_LINK_UPDATE_EXP
+                       : mode == LQ_SYMPLECTIC_EXP_REUNITARIZE ? LQ_LINK_UPDATE_EXP_REUNITARIZE
+                                                               : LQ_LINK_UPDATE_EULER;
+        int rc = run_symplectic(st, st.cur, dt, n, false, lu, &fin);
         if (rc) return rc;
         st.cur = fin;
         st.t += n;
@@ -703,7 +755,7 @@ int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_
     rc = efield_sumsq(st, 3);
     if (rc) return rc;
     int fin = -1;
-    rc = run_symplectic(st, st.cur, dt, n_steps, true, &fin); // start momenta stay in st.E
+    rc = run_symplectic(st, st.cur, dt, n_steps, true, st.link_update, &fin); // start momenta stay in st.E
     if (rc) return rc;
     double hu_old = 0.0, he_old = 0.0, hu_new = 0.0, he_new = 0.0;
     if (st.precision == LQ_PRECISION_F64) {

@@ -49,6 +49,7 @@ struct State {
 
     long long t = 0;
     int leap = 0;
+    int link_update = LQ_LINK_UPDATE_EULER; // of the HMC proposal
 
     // HMC proposal bookkeeping
     int has_pending = 0;
@@ -79,7 +80,7 @@ struct Ops {
     cudaError_t (*links_cold)(State &s, void *dst);
     cudaError_t (*links_random)(State &s, void *dst, uint64_t seed);
     cudaError_t (*efield_from_aos)(State &s, const double *d_aos);
-    cudaError_t (*efield_to_aos)(State &s, double *d_aos);
+    cudaError_t (*efield_to_aos)(State &s, const void *E, double *d_aos);
     cudaError_t (*efield_normal)(State &s, uint64_t seed, uint64_t counter, double sd);
     // md: mode bits MD_KICK | MD_DRIFT | MD_DRIFT_OLD_E; h1, h2 kick step sizes; dt drift step;
     // E is read from Ein and written to Eout (equal for an in-place update)
@@ -102,6 +103,10 @@ struct Ops {
     cudaError_t (*normalize)(State &s, void *U);
     // finalize NV rows of n partials into d_out[offset..]
     cudaError_t (*finalize)(State &s, int nv, uint32_t n, int offset);
+    // out (an E-field buffer, zeroed) <- scale * Im Tr(T^a U Sigma) per link
+    cudaError_t (*force)(State &s, const void *U, void *out, double scale);
+    // U_mu(site) <- exp(i angle T^a) U_mu(site)
+    cudaError_t (*link_rotate)(State &s, void *U, uint32_t site, int mu, int a, double angle);
 };
 
 const Ops *ops_f64(int dim);

@@ -183,6 +183,127 @@ template <typename T> __device__ __forceinline__ void im_tr_generators(const mat
     out[7] = T(kOneOver2Sqrt3) * (x.e[0].im + x.e[4].im) + T(kMinusOneOverSqrt3) * x.e[8].im;
 }
 
+// 1/n! evaluated at compile time
+constexpr double inv_factorial(int n) {
+    double f = 1.0;
+    for (int k = 2; k <= n; ++k) f *= (double)k;
+    return 1.0 / f;
+}
+
+// exp(i X) - 1 for X = sum_a v^a T^a, by the Cayley-Hamilton recursion of su3_exp_i
+// (src/su3.rs:832-855; the method of the OpenQCD su3_fcts notes): exp(i X) = q0 + q1 X + q2 X^2
+// with, from q0 = 1/(N-1)!, q1 = q2 = 0 and for i = N-2 down to 0,
+//   q0 <- 1/i! + d q2,  q1 <- i (q0 - t q2),  q2 <- i q1,   d = i det X,  t = -Tr(X^2)/2.
+// The identity (the 1/0! of the last step) is left out so that a small rotation keeps its
+// relative precision.  N = 26 terms as the reference for double; 18 for float, where
+// 1/(N-7)! is below the FP32 epsilon (the reference's criterion, src/su3.rs:716-725).
+template <typename T> __device__ __forceinline__ void su3_exp_i_minus_one(const T *v, mat3<T> &r) {
+    constexpr int NL = (sizeof(T) == 8 ? 26 : 18) - 1;
+    mat3<T> m;
+    adjoint_to_matrix<T>(v, m);
+    // det of the Hermitian X is real: expansion along the first row
+    const cpx<T> c0 = cmk(m.e[4].re * m.e[8].re - (m.e[5].re * m.e[5].re + m.e[5].im * m.e[5].im), T(0));
+    // m.e[1] * (m.e[3] m.e[8] - m.e[5] m.e[6]) and m.e[2] * (m.e[3] m.e[7] - m.e[4] m.e[6])
+    const T a_re = m.e[3].re * m.e[8].re - (m.e[5].re * m.e[6].re - m.e[5].im * m.e[6].im);
+    const T a_im = m.e[3].im * m.e[8].re - (m.e[5].re * m.e[6].im + m.e[5].im * m.e[6].re);
+    const T b_re = (m.e[3].re * m.e[7].re - m.e[3].im * m.e[7].im) - m.e[4].re * m.e[6].re;
+    const T b_im = (m.e[3].re * m.e[7].im + m.e[3].im * m.e[7].re) - m.e[4].re * m.e[6].im;
+    const T det = m.e[0].re * c0.re - (m.e[1].re * a_re - m.e[1].im * a_im) + (m.e[2].re * b_re - m.e[2].im * b_im);
+    T ts = T(0);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) ts = fma(v[a], v[a], ts);
+    const T t = T(-0.25) * ts; // -Tr(X^2)/2 = -(sum v^2 / 2) / 2
+    T inv = T(inv_factorial(NL));
+    T q0r = inv, q0i = T(0), q1r = T(0), q1i = T(0), q2r = T(0), q2i = T(0);
+#pragma unroll
+    for (int i = NL - 1; i >= 0; --i) {
+        inv *= T(i + 1);
+        const T c = (i == 0) ? T(0) : inv;
+        const T n0r = c - det * q2i, n0i = det * q2r;
+        const T n1r = -(q0i - t * q2i), n1i = q0r - t * q2r;
+        const T n2r = -q1i, n2i = q1r;
+        q0r = n0r;
+        q0i = n0i;
+        q1r = n1r;
+        q1i = n1i;
+        q2r = n2r;
+        q2i = n2i;
+    }
+    mat3<T> m2;
+    mul_nn(m, m, m2);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        T re = q1r * m.e[k].re - q1i * m.e[k].im;
+        T im = q1r * m.e[k].im + q1i * m.e[k].re;
+        re = fma(q2r, m2.e[k].re, fma(-q2i, m2.e[k].im, re));
+        im = fma(q2r, m2.e[k].im, fma(q2i, m2.e[k].re, im));
+        r.e[k] = cmk(re, im);
+    }
+    r.e[0].re += q0r;
+    r.e[0].im += q0i;
+    r.e[4].re += q0r;
+    r.e[4].im += q0i;
+    r.e[8].re += q0r;
+    r.e[8].im += q0i;
+}
+
+// orthonormalize_matrix (src/su3.rs:290-309) in double on a row-major 3x3 (re, im):
+// v1 = col0 / |col0|, v2 = col1 - v1 (v1^* . col1), normalised, col2 = conj(v1) x conj(v2);
+// a vector whose norm is <= f64::EPSILON is kept unnormalised (try_normalize).
+__device__ __forceinline__ void orthonormalize_d(double (&re)[9], double (&im)[9]) {
+    double r1[3], i1[3], r2[3], i2[3];
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+        r1[row] = re[row * 3];
+        i1[row] = im[row * 3];
+        r2[row] = re[row * 3 + 1];
+        i2[row] = im[row * 3 + 1];
+    }
+    const double eps = 2.220446049250313e-16;
+    const double n1 = sqrt(r1[0] * r1[0] + i1[0] * i1[0] + r1[1] * r1[1] + i1[1] * i1[1] + r1[2] * r1[2] + i1[2] * i1[2]);
+    if (n1 > eps) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            r1[k] /= n1;
+            i1[k] /= n1;
+        }
+    }
+    double pr = 0.0, pi = 0.0; // sum_k conj(v1_k) v2_k
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        pr += r1[k] * r2[k] + i1[k] * i2[k];
+        pi += r1[k] * i2[k] - i1[k] * r2[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        r2[k] -= r1[k] * pr - i1[k] * pi;
+        i2[k] -= r1[k] * pi + i1[k] * pr;
+    }
+    const double n2 = sqrt(r2[0] * r2[0] + i2[0] * i2[0] + r2[1] * r2[1] + i2[1] * i2[1] + r2[2] * r2[2] + i2[2] * i2[2]);
+    if (n2 > eps) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            r2[k] /= n2;
+            i2[k] /= n2;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+        // (a x b)_k with a = conj(v1), b = conj(v2)
+        const double xr = r1[k1] * r2[k2] - i1[k1] * i2[k2];
+        const double xi = -(r1[k1] * i2[k2] + i1[k1] * r2[k2]);
+        const double yr = r1[k2] * r2[k1] - i1[k2] * i2[k1];
+        const double yi = -(r1[k2] * i2[k1] + i1[k2] * r2[k1]);
+        re[k * 3] = r1[k];
+        im[k * 3] = i1[k];
+        re[k * 3 + 1] = r2[k];
+        im[k * 3 + 1] = i2[k];
+        re[k * 3 + 2] = xr - yr;
+        im[k * 3 + 2] = xi - yi;
+    }
+}
+
 // ---- tiled structure-of-arrays storage ----
 // Sites are grouped in tiles of 32 consecutive sites (one warp).  An array of P planes stores
 // plane p of site s at ((s / 32) * P + p) * 32 + s % 32: within a tile all planes of a site

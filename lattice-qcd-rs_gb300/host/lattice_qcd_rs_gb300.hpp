@@ -420,6 +420,25 @@ class SymplecticEulerGpu {
     }
 };
 
+// ------------------------------------------------------------------ differentiation
+// The Wilson action as an autograd-style function: forward gives S = beta sum (1 - Re Tr P / 3),
+// backward the gradient dS/dtheta^a for U -> exp(i theta^a T^a) U on every link, in the E-field
+// layout.  The reference's force derivative_e (src/simulation/state.rs:1420-1448) is
+// -sqrt(2 C_A)/(size beta) times the gradient.
+template <int D> struct WilsonAction {
+    static Real forward(const LatticeStateDefault<D> &s) {
+        double v = 0.0;
+        check(lq_wilson_action(s.raw(), &v), "lq_wilson_action");
+        return v;
+    }
+    static EField<D> backward(const LatticeStateDefault<D> &s) {
+        EField<D> g;
+        g.data.resize(s.lattice().number_of_points() * D * 8);
+        check(lq_wilson_action_backward(s.raw(), g.data.data(), g.data.size()), "lq_wilson_action_backward");
+        return g;
+    }
+};
+
 // ------------------------------------------------------------------ HMC driver
 // HybridMonteCarloDiagnostic<LatticeStateDefault<D>, Rng, I, D>
 // (src/simulation/monte_carlo/hybrid_monte_carlo.rs:302-614).  next_element draws the momenta

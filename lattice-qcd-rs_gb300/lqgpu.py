@@ -31,7 +31,8 @@ globals().update({v: k for k, v in STATUS.items()})
 PRECISION_F64 = 0
 PRECISION_MIXED = 1
 PRECISION_F32 = 2
-SYNC_SYNC, SYNC_LEAP, LEAP_LEAP, LEAP_SYNC, SYMPLECTIC = range(5)
+SYNC_SYNC, SYNC_LEAP, LEAP_LEAP, LEAP_SYNC, SYMPLECTIC, SYMPLECTIC_EXP, SYMPLECTIC_EXP_REUNITARIZE = range(7)
+LINK_UPDATE_EULER, LINK_UPDATE_EXP, LINK_UPDATE_EXP_REUNITARIZE = range(3)
 
 # every symbol the header declares, with (restype, argtypes)
 _vp, _i32, _u64, _f64, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double, ctypes.c_size_t
@@ -46,6 +47,7 @@ SIGNATURES = {
     "lq_state_set_stream": (_i32, [_vp, _vp]),
     "lq_state_info": (_i32, [_vp, _ip, _ip, _dp, _dp, _ip, _llp, _llp, _ip]),
     "lq_state_set_beta": (_i32, [_vp, _f64]),
+    "lq_state_set_link_update": (_i32, [_vp, _i32]),
     "lq_state_device_bytes": (_i32, [_vp, _szp]),
     "lq_links_upload": (_i32, [_vp, _dp, _sz]),
     "lq_links_download": (_i32, [_vp, _dp, _sz]),
@@ -71,6 +73,9 @@ SIGNATURES = {
     "lq_hmc_decide": (_i32, [_vp, _i32]),
     "lq_hmc_trajectory": (_i32, [_vp, _f64, _i32, _u64, _u64, _f64, _i32, _ip, _dp, _dp, _ip]),
     "lq_plaquette_sums_noalloc": (_i32, [_i32, _i32, _vp, _vp, _vp]),
+    "lq_wilson_action": (_i32, [_vp, _dp]),
+    "lq_wilson_action_backward": (_i32, [_vp, _dp, _sz]),
+    "lq_link_rotate": (_i32, [_vp, ctypes.c_longlong, _i32, _f64]),
     "lq_profile_enable": (_i32, [_vp, _i32]),
     "lq_profile_read": (_i32, [_vp, _i32, _llp, _dp, _i32]),
     "lq_status_string": (ctypes.c_char_p, [_i32]),
@@ -176,6 +181,9 @@ class State:
     def set_beta(self, beta):
         _check(load().lq_state_set_beta(self._h, beta), "lq_state_set_beta")
 
+    def set_link_update(self, link_update):
+        _check(load().lq_state_set_link_update(self._h, link_update), "lq_state_set_link_update")
+
     @property
     def t(self):
         return self.info()["t"]
@@ -244,6 +252,18 @@ class State:
         out = np.empty((self.n_sites, 8))
         _check(load().lq_gauss_download(self._h, _p(out), out.size), "lq_gauss_download")
         return out
+
+    # ---- differentiation
+    def wilson_action(self):
+        return self._scalar(load().lq_wilson_action, "lq_wilson_action")
+
+    def wilson_action_backward(self):
+        out = np.empty((self.n_sites, self.dim, 8))
+        _check(load().lq_wilson_action_backward(self._h, _p(out), out.size), "lq_wilson_action_backward")
+        return out
+
+    def link_rotate(self, link, generator, angle):
+        _check(load().lq_link_rotate(self._h, link, generator, angle), "lq_link_rotate")
 
     # ---- updates
     def project_to_gauss(self, max_steps=100000):

@@ -42,7 +42,9 @@ enum {
     OR_SYNC_LEAP = 1,
     OR_LEAP_LEAP = 2,
     OR_LEAP_SYNC = 3,
-    OR_SYMPLECTIC = 4
+    OR_SYMPLECTIC = 4,
+    OR_SYMPLECTIC_EXP = 5,            /* symplectic with U' = su3_exp_i(dt sqrt(6)/size E) U */
+    OR_SYMPLECTIC_EXP_NORMALIZE = 6   /* the same, then orthonormalize_matrix on every link */
 };
 
 /* ---- random numbers: Xoshiro256++ seeded through SplitMix64 ---- */

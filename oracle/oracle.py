@@ -24,7 +24,7 @@ OR_ERR_ZERO_INTEGRATION = 8
 OR_ERR_INVALID_ARGUMENT = 9
 OR_ERR_NOT_CONVERGED = 10
 
-SYNC_SYNC, SYNC_LEAP, LEAP_LEAP, LEAP_SYNC, SYMPLECTIC = range(5)
+SYNC_SYNC, SYNC_LEAP, LEAP_LEAP, LEAP_SYNC, SYMPLECTIC, SYMPLECTIC_EXP, SYMPLECTIC_EXP_NORMALIZE = range(7)
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _lib = None

@@ -79,6 +79,22 @@ int main() {
         CHECK(next.t() == 1);
     }
 
+    // the action's backward against a central difference on one link and generator
+    {
+        auto rng = Xoshiro256PlusPlus::seed_from_u64(2);
+        auto st = LatticeStateDefault<4>::new_determinist(1.0, 2.0, 4, rng).unwrap();
+        const EField<4> g = WilsonAction<4>::backward(st);
+        const long long link = 37;
+        const int a = 5;
+        const double eps = 1e-5;
+        check(lq_link_rotate(st.raw(), link, a, eps), "rotate");
+        const double sp = WilsonAction<4>::forward(st);
+        check(lq_link_rotate(st.raw(), link, a, -2 * eps), "rotate");
+        const double sm = WilsonAction<4>::forward(st);
+        const double fd = (sp - sm) / (2 * eps);
+        CHECK(std::fabs(fd - g.data[(std::size_t)link * 8 + a]) < 1e-4);
+    }
+
     // setter with a wrong size panics, as the reference's set_link_matrix does
     {
         auto s = LatticeStateDefault<2>::new_cold(1.0, 1.0, 4).unwrap();

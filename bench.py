@@ -217,6 +217,30 @@ def algorithmic_md_bytes(n_links, md_steps, real_bytes):
     return n_links * real_bytes * (52 * md_steps + 34)
 
 
+def rank_reducers(pg, device):
+    """(barrier, max_over_ranks, sum_over_ranks) for the replicas; identities without a group."""
+    import torch
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    def reduce(x, op):
+        if pg is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        pg.all_reduce(t, op=op)
+        return float(t.item())
+
+    return (barrier, lambda x: reduce(x, pg.ReduceOp.MAX if pg else None),
+            lambda x: reduce(x, pg.ReduceOp.SUM if pg else None))
+
+
+def replica_value(units, ms, max_over_ranks, sum_over_ranks):
+    """whole-job throughput: every rank's units over the slowest rank's time"""
+    return sum_over_ranks(units) / (max_over_ranks(ms) / 1000.0)
+
+
 def run_ours(args):
     rank, world, local_rank = dist_env()
     if world > 1:
@@ -244,23 +268,7 @@ def run_ours(args):
     real_bytes = 4 if prec == lqgpu.PRECISION_F32 else 8
     uni = np.random.default_rng(1000 + rank)
 
-    def barrier():
-        if pg is not None:
-            pg.barrier()
-
-    def max_over_ranks(x):
-        if pg is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum_over_ranks(x):
-        if pg is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.SUM)
-        return float(t.item())
+    barrier, max_over_ranks, sum_over_ranks = rank_reducers(pg, dev)
 
     def timed_trajectories(state, k_warm, k_timed, seed, sample_clocks=False):
         results = []
@@ -294,7 +302,7 @@ def run_ours(args):
     s.profile_enable(True)
     ms, wall, prof, res, clocks = timed_trajectories(s, args.warmup, args.steps, 77 + rank, sample_clocks=True)
     ms_max = max_over_ranks(ms)
-    value = sum_over_ranks(n_links * nmd * args.steps) / (ms_max / 1000.0)
+    value = replica_value(n_links * nmd * args.steps, ms, max_over_ranks, sum_over_ranks)
     launches = sum(v[0] for v in prof.values())
     md_launches, md_ms = prof["md"]
     md_bytes = algorithmic_md_bytes(n_links, nmd, real_bytes) * args.steps

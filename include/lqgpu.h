@@ -186,6 +186,25 @@ int lq_wilson_action_backward(lq_state *s, double *grad, size_t n_doubles);
  * finite-difference probes of the action */
 int lq_link_rotate(lq_state *s, long long link, int generator, double angle);
 
+/* Reverse-mode adjoint of a leap-frog trajectory.  No counterpart in the reference.
+ * Runs n_steps symplectic steps (LQ_SYMPLECTIC with the reference's first-order link update,
+ * the HMC proposal's integrator) from the state's links U0 and momenta E0 -- the state itself
+ * is left unchanged -- and differentiates
+ *   objective O = Re average_trace_plaquette(U_n) / 3
+ * backwards through every kick and drift: grad_links = dO/dU0 as a complex cotangent per
+ * link (dO/dRe U + i dO/dIm U, serde link layout), grad_efield = dO/dE0 (E-field layout), and
+ *   d_objective_d_beta = dO/dbeta for momenta drawn by scaling one fixed normal field,
+ *   E0(beta) = E0 beta0 / beta (the standard deviation is 0.5/beta); the molecular dynamics
+ *   itself does not depend on beta (the reference's force has no beta factor).
+ * Memory: checkpoints of the state entering every c-th step (c = checkpoint_every, 0: the
+ * default ceil(sqrt(n_steps))), each segment recomputed once in the reverse pass; work_bytes
+ * returns the device bytes of this work (allocated for the call and freed before it returns).
+ * The FP32 forms run the adjoint in FP32 on the hi parts of the links and momenta.
+ * Outputs may be NULL; n_*_doubles as lq_links_download / lq_efield_download. */
+int lq_leapfrog_adjoint(lq_state *s, double dt, int n_steps, int checkpoint_every, double *objective,
+                        double *d_objective_d_beta, double *grad_links, size_t n_link_doubles, double *grad_efield,
+                        size_t n_efield_doubles, size_t *work_bytes);
+
 /* ---------------------------------------------------------------- HMC
  * HybridMonteCarloDiagnostic::next_element (src/simulation/monte_carlo/hybrid_monte_carlo.rs:465-471,
  * :573-613), split as the reference splits it:
@@ -241,6 +260,76 @@ int lq_profile_read(lq_state *s, int kernel_class, long long *launches, double *
  * array's device address with that device current; make that first call before any stream
  * capture. */
 int lq_plaquette_sums_noalloc(int dim, int L, const double *d_links, double *d_out, void *stream);
+
+/* ---------------------------------------------------------------- batched ensembles
+ * The reference's parameter-scan use: many independent HybridMonteCarloDiagnostic runs
+ * (src/simulation/monte_carlo/hybrid_monte_carlo.rs:465-471, :573-613), one
+ * LatticeStateDefault<D> each (src/simulation/state.rs:577-641), of uneven side length and
+ * beta.  The reference runs them one after another; here every ensemble of a batch lives in
+ * one set of device arrays and each kernel of a trajectory covers all of them (a per-ensemble
+ * offset table), so small lattices do not leave the GPU idle.  An ensemble's trajectory is the
+ * same arithmetic as lq_hmc_trajectory of a state of the same precision, with
+ *   momenta      : lq_hmc_refresh's device draw, seed = batch seed + ensemble index, counter =
+ *                  the ensemble's trajectory counter (lq_batch_set_seed sets both)
+ *   accept test  : uniform = the 53-bit Philox value of counter block (0xFFFFFFFF, counter lo,
+ *                  counter hi, 4) under the ensemble's key, recorded in the results
+ *   Delta H      : -beta/3 sum Re Tr[P' - P] + beta/2 sum (e'^2 - e^2) from difference kernels,
+ *                  for every precision (lq_hmc_propose subtracts two Hamiltonians for FP64)
+ *   projection   : fused sweeps for every precision (the FP64 state uses two kernels per step),
+ *                  per ensemble until its own residual test passes; max_gauss_steps <= 0 means
+ *                  10001 (the device loop needs a bound).
+ * Ensembles whose projection fails (NaN: LQ_ERR_GAUSS_PROJECTION, or the step limit:
+ * LQ_ERR_NOT_CONVERGED) keep their links for that trajectory; the status is in the results. */
+typedef struct lq_batch lq_batch;
+enum lq_batch_flags {
+    LQ_BATCH_USE_GRAPH = 1,         /* replay one captured CUDA graph per trajectory */
+    LQ_BATCH_MEASURE_PLAQUETTE = 2  /* record average_trace_plaquette of every ensemble after each trajectory */
+};
+/* kernel classes of lq_batch_tuning */
+enum lq_batch_kernel_class {
+    LQ_BATCH_KERNEL_MD = 0,
+    LQ_BATCH_KERNEL_SWEEP = 1,
+    LQ_BATCH_KERNEL_GAUSS = 2,
+    LQ_BATCH_KERNEL_PLAQUETTE_DELTA = 3,
+    LQ_BATCH_KERNEL_SUMSQ_DELTA = 4,
+    LQ_BATCH_KERNEL_NORMAL = 5,
+    LQ_BATCH_KERNEL_PLAQUETTE = 6,
+    LQ_BATCH_KERNEL_CLASSES = 7
+};
+/* n ensembles of dimension dim: ensemble e has L[e] points per direction, lattice size size[e]
+ * and beta[e]; cold links.  Errors as lq_state_create, checked per ensemble. */
+int lq_batch_create(int dim, int n_ensembles, const int *L, const double *size, const double *beta, int precision,
+                    lq_batch **out);
+int lq_batch_destroy(lq_batch *b);
+int lq_batch_set_stream(lq_batch *b, void *stream);
+int lq_batch_info(const lq_batch *b, int *dim, int *n_ensembles, long long *total_links, size_t *device_bytes);
+int lq_batch_set_link_update(lq_batch *b, int link_update);
+/* Philox keys seed + e and trajectory counters of every ensemble */
+int lq_batch_set_seed(lq_batch *b, uint64_t seed, uint64_t counter);
+/* ensemble e <- lq_links_random(seed + e) */
+int lq_batch_links_random(lq_batch *b, uint64_t seed);
+/* one ensemble's links in the serde layout, n = L[e]^dim * dim * 18 doubles */
+int lq_batch_links_upload(lq_batch *b, int ensemble, const double *links, size_t n_doubles);
+int lq_batch_links_download(lq_batch *b, int ensemble, double *links, size_t n_doubles);
+int lq_batch_normalize_link_matrices(lq_batch *b);
+/* average_trace_plaquette of every ensemble: re[e], im[e] */
+int lq_batch_average_trace_plaquette(lq_batch *b, double *re, double *im);
+/* Times each kernel class under candidate launch shapes (one block per work item, or 1, 2, 4, 8
+ * waves of resident blocks; directions-fastest or chunks-fastest work order) on the batch's
+ * own data and keeps the fastest.  The links are not changed; results of later trajectories do
+ * not depend on the shapes. */
+int lq_batch_autotune(lq_batch *b, double dt, int reps);
+int lq_batch_tuning(const lq_batch *b, int kernel_class, int *grid, int *order, double *ms);
+/* n_trajectories HMC trajectories (n_steps leap-frog steps of dt) of every ensemble; results
+ * rows 0..n_trajectories-1 of this run. */
+int lq_batch_hmc_run(lq_batch *b, double dt, int n_steps, int n_trajectories, int max_gauss_steps, int flags);
+/* rows first..first+count-1 of the last run, each array (optional) count * n_ensembles,
+ * row-major: delta_h, prob, uniform, accepted, gauss_steps, status, plaquette (<Re Tr P> after
+ * the trajectory, with LQ_BATCH_MEASURE_PLAQUETTE) */
+int lq_batch_hmc_results(lq_batch *b, int first, int count, double *delta_h, double *prob, double *uniform,
+                         int *accepted, int *gauss_steps, int *status, double *plaquette);
+/* graph launches since creation */
+int lq_batch_graph_launches(const lq_batch *b, long long *launches);
 
 /* ---------------------------------------------------------------- diagnostics */
 const char *lq_status_string(int status);

@@ -2,6 +2,7 @@
 #pragma once
 #include <math.h>
 
+#include "adjoint.cuh"
 #include "kernels.cuh"
 #include "state.hpp"
 
@@ -20,13 +21,16 @@ template <int D, typename T, bool COMP> struct Engine {
         return g;
     }
     static dim3 link_grid(const State &s, int threads) { return dim3((s.V + threads - 1) / threads, D, 1); }
+    // distance in elements from the hi array to the lo array of compensated links / E-field
+    static size_t ulo(const State &s) { return (size_t)tiles_of(s.V) * D * 9 * kTile; }
+    static size_t elo(const State &s) { return (size_t)tiles_of(s.V) * D * 8 * kTile; }
 
     static cudaError_t links_from_aos(State &s, const double *d_aos, void *dst) {
-        k_links_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (V2<T> *)dst, s.V);
+        k_links_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (V2<T> *)dst, s.V, ulo(s));
         return cudaGetLastError();
     }
     static cudaError_t links_to_aos(State &s, const void *src, double *d_aos) {
-        k_links_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)src, d_aos, s.V);
+        k_links_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)src, d_aos, s.V, ulo(s));
         return cudaGetLastError();
     }
     static cudaError_t links_cold(State &s, void *dst) {
@@ -38,18 +42,18 @@ template <int D, typename T, bool COMP> struct Engine {
     }
     static cudaError_t links_random(State &s, void *dst, uint64_t seed) {
         const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-        k_links_random<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, s.V, key);
+        k_links_random<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, s.V, key, ulo(s));
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        k_normalize<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, geo(s));
+        k_normalize<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)dst, geo(s), ulo(s));
         return cudaGetLastError();
     }
     static cudaError_t efield_from_aos(State &s, const double *d_aos) {
-        k_efield_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V);
+        k_efield_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V, elo(s));
         return cudaGetLastError();
     }
     static cudaError_t efield_to_aos(State &s, const void *E, double *d_aos) {
-        k_efield_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)E, d_aos, s.V);
+        k_efield_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)E, d_aos, s.V, elo(s));
         return cudaGetLastError();
     }
     // out <- scale * Im Tr(T^a U_mu(x) Sigma_mu(x)) on every link (out zeroed by the caller)
@@ -152,7 +156,7 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
     static cudaError_t normalize(State &s, void *U) {
-        k_normalize<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)U, geo(s));
+        k_normalize<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((V2<T> *)U, geo(s), ulo(s));
         return cudaGetLastError();
     }
     static cudaError_t finalize(State &s, int nv, uint32_t n, int offset) {
@@ -164,11 +168,45 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
 
+    // ---- reverse-mode adjoint of the leap-frog (hi parts of compensated arrays)
+    static dim3 md_grid(const State &s) { return dim3(((s.V + 127) / 128) * D, 1, 1); }
+    static cudaError_t adj_init(State &s, const void *U, void *lamU, double scale) {
+        k_adj_init<D, T><<<md_grid(s), 128, 0, s.stream>>>((const V2<T> *)U, (V2<T> *)lamU, geo(s), (T)scale);
+        return cudaGetLastError();
+    }
+    static cudaError_t adj_kick(State &s, const void *U, const void *lamE, void *lamU, double coef) {
+        k_adj_kick<D, T><<<md_grid(s), 128, 0, s.stream>>>((const V2<T> *)U, (const T *)lamE, (V2<T> *)lamU, geo(s),
+                                                           (T)coef);
+        return cudaGetLastError();
+    }
+    static cudaError_t adj_drift(State &s, const void *U, const void *E, void *lamU, void *lamE, double kappa) {
+        k_adj_drift<D, T><<<md_grid(s), 128, 0, s.stream>>>((const V2<T> *)U, (const T *)E, (V2<T> *)lamU,
+                                                            (T *)lamE, s.V, (T)kappa);
+        return cudaGetLastError();
+    }
+    static cudaError_t dot(State &s, const void *a, const void *b, uint32_t *n_partials) {
+        const uint32_t blocks = 1024;
+        k_dot<T><<<blocks, 256, 0, s.stream>>>((const T *)a, (const T *)b, s.efield_elems(), s.partial);
+        *n_partials = blocks;
+        return cudaGetLastError();
+    }
+    // cotangent arrays (no compensated part) to the serde layouts
+    static cudaError_t cot_links_to_aos(State &s, const void *lamU, double *d_aos) {
+        k_links_to_aos<D, T, false><<<link_grid(s, 128), 128, 0, s.stream>>>((const V2<T> *)lamU, d_aos, s.V, 0);
+        return cudaGetLastError();
+    }
+    static cudaError_t cot_efield_to_aos(State &s, const void *lamE, double *d_aos) {
+        k_efield_to_aos<D, T, false><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)lamE, d_aos, s.V, 0);
+        return cudaGetLastError();
+    }
+
     static const Ops *table() {
         static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
                                 efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
                                 gauss_step,     gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
-                                normalize,      finalize,       force,         link_rotate};
+                                normalize,      finalize,       force,         link_rotate,
+                                adj_init,       adj_kick,       adj_drift,     dot,
+                                cot_links_to_aos, cot_efield_to_aos};
         return &ops;
     }
 };

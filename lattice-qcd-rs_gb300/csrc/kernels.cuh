@@ -146,7 +146,7 @@ __device__ __forceinline__ void staple_sum(const V2<T> *__restrict__ U, const Ge
 
 enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4, MD_EXP = 8, MD_REUNIT = 16 };
 
-// One thread per link.  Blocks are ordered with mu fastest (blockIdx.x = site_block*D + mu)
+// k_md: one thread per link.  Blocks are ordered with mu fastest (blockIdx.x = site_block*D + mu)
 // so the D directions of a block of sites run together and the neighbour links they share
 // stay in L2.
 //  KICK : F^a = Im Tr(T^a U_mu(x) Sigma(x)) (derivative_e, src/simulation/state.rs:1420-1448);
@@ -161,14 +161,12 @@ enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4, MD_EXP = 8, MD_REUNI
 //         With EXP the link moves on the group instead: U' = exp(i drift E) U, the
 //         exponential by su3_exp_i's Cayley-Hamilton recursion; REUNIT then applies
 //         orthonormalize_matrix to the result (in double, from hi + lo).
+// md_link computes link (site, mu); ulo / elo: distance in elements from a hi array to its
+// lo array (compensated storage).
 template <int D, typename T, bool COMP, int MODE>
-__global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout,
-                                  Geo<D> g, T k1, T k2, T drift) {
-    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
-    const int mu = blockIdx.x % D;
-    if (site >= g.V) return;
-    const size_t nt = tiles_of(g.V);
-    const size_t elo = nt * D * 8 * kTile, ulo = nt * D * 9 * kTile;
+__device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein,
+                                        T *Eout, const Geo<D> &g, uint32_t site, int mu, T k1, T k2, T drift,
+                                        size_t ulo, size_t elo) {
     // the staple sum first: the link and momenta of (x, mu) are loaded after it so they do
     // not occupy registers while the neighbour links are in flight
     mat3<T> sig;
@@ -259,6 +257,16 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
         store_mat<T>(Uout + ui, u);
     }
 }
+template <int D, typename T, bool COMP, int MODE>
+__global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout,
+                                  Geo<D> g, T k1, T k2, T drift) {
+    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.x % D;
+    if (site >= g.V) return;
+    const size_t nt = tiles_of(g.V);
+    md_link<D, T, COMP, MODE>(Uin, Uout, Ein, Eout, g, site, mu, k1, k2, drift, nt * D * 9 * kTile,
+                              nt * D * 8 * kTile);
+}
 
 // U <- exp(i angle T^a) U for one link (finite-difference probes of the action)
 template <int D, typename T, bool COMP>
@@ -327,11 +335,9 @@ template <typename T> __device__ __forceinline__ void herm_store(T *__restrict__
 // g^a = 2 Re Tr(T^a G) (gauss_sum_div, src/field.rs:1199-1220), is reduced into one
 // partial per block.  Reads hi parts only.
 template <int D, typename T>
-__global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, const T *__restrict__ E,
-                                               T *__restrict__ G, Geo<D> g, double *__restrict__ partial) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    double r[1] = {0.0};
-    if (site < g.V) {
+__device__ __forceinline__ double gauss_site(const V2<T> *__restrict__ U, const T *__restrict__ E, T *__restrict__ G,
+                                             const Geo<D> &g, uint32_t site) {
+    {
         uint32_t c[D];
         site_coords(g, site, c);
         mat3<T> gs;
@@ -363,8 +369,15 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
         T s = T(0);
 #pragma unroll
         for (int a = 0; a < 8; ++a) s += gc[a];
-        r[0] = (double)(fabs(s) * T(0.5));
+        return (double)(fabs(s) * T(0.5));
     }
+}
+template <int D, typename T>
+__global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, const T *__restrict__ E,
+                                               T *__restrict__ G, Geo<D> g, double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double r[1] = {0.0};
+    if (site < g.V) r[0] = gauss_site<D, T>(U, E, G, g, site);
     block_reduce_store<1>(r, partial, blockIdx.x, gridDim.x);
 }
 
@@ -430,13 +443,10 @@ __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U,
 // neighbours' old values while they are being replaced).  U is read once per sweep instead
 // of twice (Gauss law, then step) and the sweep needs one launch instead of two.
 template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
-                                                     T *__restrict__ Eout, const T *__restrict__ Gin,
-                                                     T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    double r[1] = {0.0};
-    if (site < g.V) {
-        const size_t elo = (size_t)tiles_of(g.V) * D * 8 * kTile;
+__device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
+                                             T *__restrict__ Eout, const T *__restrict__ Gin, T *__restrict__ Gout,
+                                             const Geo<D> &g, uint32_t site, size_t elo) {
+    {
         uint32_t c[D];
         site_coords(g, site, c);
         mat3<T> gx, gnew;
@@ -499,8 +509,17 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const 
         T sum = T(0);
 #pragma unroll
         for (int a = 0; a < 8; ++a) sum += gc[a];
-        r[0] = (double)(fabs(sum) * T(0.5));
+        return (double)(fabs(sum) * T(0.5));
     }
+}
+template <int D, typename T, bool COMP>
+__global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
+                                                     T *__restrict__ Eout, const T *__restrict__ Gin,
+                                                     T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double r[1] = {0.0};
+    if (site < g.V)
+        r[0] = sweep_site<D, T, COMP>(U, Ein, Eout, Gin, Gout, g, site, (size_t)tiles_of(g.V) * D * 8 * kTile);
     block_reduce_store<1>(r, partial, blockIdx.x, gridDim.x);
 }
 
@@ -512,11 +531,9 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const 
 // (average_trace_plaquette, src/field.rs:775-804).  The traces of one site accumulate in
 // T (hi parts of compensated links) and every sum over sites in double.
 template <int D, typename T>
-__global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, Geo<D> g,
-                                                   double *__restrict__ partial) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[3] = {0.0, 0.0, 0.0};
-    if (site < g.V) {
+__device__ __forceinline__ void plaquette_site(const V2<T> *__restrict__ U, const Geo<D> &g, uint32_t site,
+                                               double (&v)[3]) {
+    {
         uint32_t c[D];
         site_coords(g, site, c);
         T sre = T(0), sim = T(0), sh = T(0);
@@ -549,6 +566,13 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
         v[1] = (double)sre;
         v[2] = (double)sim;
     }
+}
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, Geo<D> g,
+                                                   double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if (site < g.V) plaquette_site<D, T>(U, g, site, v);
     block_reduce_store<3>(v, partial, blockIdx.x, gridDim.x);
 }
 
@@ -560,12 +584,9 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
 // proportional to |dU|, not to |U|.  dU = (hi' - hi) + (lo' - lo) keeps the compensated part.
 // Partial: sum Re Tr(P' - P) (Delta hamiltonian_links = -beta/3 times it).
 template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
-                                                         Geo<D> g, double *__restrict__ partial) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[1] = {0.0};
-    if (site < g.V) {
-        const size_t ulo = (size_t)tiles_of(g.V) * D * 9 * kTile;
+__device__ __forceinline__ double plaquette_delta_site(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
+                                                       const Geo<D> &g, uint32_t site, size_t ulo) {
+    {
         uint32_t c[D];
         site_coords(g, site, c);
         auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
@@ -643,8 +664,16 @@ __global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict
                 acc += term;
             }
         }
-        v[0] = (double)acc;
+        return (double)acc;
     }
+}
+template <int D, typename T, bool COMP>
+__global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
+                                                         Geo<D> g, double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (site < g.V)
+        v[0] = plaquette_delta_site<D, T, COMP>(Uo, Un, g, site, (size_t)tiles_of(g.V) * D * 9 * kTile);
     block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
 }
 
@@ -682,12 +711,11 @@ __global__ void __launch_bounds__(256) k_sum_squares_delta(const T *__restrict__
 // v1 = col0 / |col0|, v2 = col1 - v1 (v1^* . col1), normalised, col2 = conj(v1) x conj(v2);
 // a vector whose norm is <= f64::EPSILON is kept unnormalised (try_normalize).
 template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D> g) {
+__global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D> g, size_t ulo) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= g.V) return;
     const size_t p0 = tix(site, D * 9, mu * 9);
-    const size_t ulo = (size_t)tiles_of(g.V) * D * 9 * kTile;
     double r1[3], i1[3], r2[3], i2[3];
 #pragma unroll
     for (int row = 0; row < 3; ++row) {
@@ -768,12 +796,11 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
 // host serde layout (double AoS, column-major complex 3x3 per link) <-> device SoA planes
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_links_from_aos(const double *__restrict__ aos, V2<T> *__restrict__ U,
-                                                        uint32_t V) {
+                                                        uint32_t V, size_t ulo) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     const double *src = aos + ((size_t)site * D + mu) * 18;
-    const size_t ulo = (size_t)tiles_of(V) * D * 9 * kTile;
     const size_t p0 = tix(site, D * 9, mu * 9);
 #pragma unroll
     for (int col = 0; col < 3; ++col)
@@ -789,12 +816,11 @@ __global__ void __launch_bounds__(128) k_links_from_aos(const double *__restrict
 }
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ U, double *__restrict__ aos,
-                                                      uint32_t V) {
+                                                      uint32_t V, size_t ulo) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     double *dst = aos + ((size_t)site * D + mu) * 18;
-    const size_t ulo = (size_t)tiles_of(V) * D * 9 * kTile;
     const size_t p0 = tix(site, D * 9, mu * 9);
 #pragma unroll
     for (int col = 0; col < 3; ++col)
@@ -814,12 +840,11 @@ __global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ 
 }
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restrict__ aos, T *__restrict__ E,
-                                                         uint32_t V) {
+                                                         uint32_t V, size_t elo) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     const double *src = aos + ((size_t)site * D + mu) * 8;
-    const size_t elo = (size_t)tiles_of(V) * D * 8 * kTile;
     const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -831,12 +856,11 @@ __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restric
 }
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, double *__restrict__ aos,
-                                                       uint32_t V) {
+                                                       uint32_t V, size_t elo) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
     double *dst = aos + ((size_t)site * D + mu) * 8;
-    const size_t elo = (size_t)tiles_of(V) * D * 8 * kTile;
     const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -918,11 +942,8 @@ __device__ __forceinline__ void box_muller(float u1, float u2, float &z0, float 
 // E^a(x, mu) ~ Normal(0, sd), independent per (link, a); counter = (link, ctr_lo, ctr_hi, call).
 // FP64 states draw 53-bit uniforms and double-precision Box-Muller; FP32 states 24-bit ones.
 template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32_t V, uint2 key, uint32_t ctr_lo,
-                                                       uint32_t ctr_hi, T sd) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    const int mu = blockIdx.y;
-    if (site >= V) return;
+__device__ __forceinline__ void efield_normal_link(T *__restrict__ E, uint32_t site, int mu, uint2 key,
+                                                   uint32_t ctr_lo, uint32_t ctr_hi, T sd, size_t elo) {
     const uint32_t link = site * D + mu;
     T z[8];
     if (sizeof(T) == 8) {
@@ -947,7 +968,6 @@ __global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32
             z[4 * j + 3] = (T)d2;
         }
     }
-    const size_t elo = (size_t)tiles_of(V) * D * 8 * kTile;
     const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -955,12 +975,20 @@ __global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32
         if (COMP) E[elo + ei + a * kTile] = T(0);
     }
 }
+template <int D, typename T, bool COMP>
+__global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32_t V, uint2 key, uint32_t ctr_lo,
+                                                       uint32_t ctr_hi, T sd) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (site >= V) return;
+    efield_normal_link<D, T, COMP>(E, site, mu, key, ctr_lo, ctr_hi, sd, (size_t)tiles_of(V) * D * 8 * kTile);
+}
 
 // random_su3 (src/su3.rs:322-355) per link: two complex 3-vectors with Uniform(-1,1)
 // entries, redrawn while |v1| <= eps or |v1 . v2| <= eps; written as columns 0 and 1, which
 // k_normalize then turns into Gram-Schmidt vectors and col2 = conj(v1) x conj(v2).
 template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uint32_t V, uint2 key) {
+__global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uint32_t V, uint2 key, size_t ulo) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     const int mu = blockIdx.y;
     if (site >= V) return;
@@ -999,7 +1027,6 @@ __global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uin
         if (hypot(dr, di) > eps) break;
     }
     const size_t p0 = tix(site, D * 9, mu * 9);
-    const size_t ulo = (size_t)tiles_of(V) * D * 9 * kTile;
 #pragma unroll
     for (int row = 0; row < 3; ++row) {
         V2<T> a, b, al, bl;

@@ -616,6 +616,112 @@ int lq_link_rotate(lq_state *s, long long link, int generator, double angle) {
     return LQ_OK;
 }
 
+// Reverse-mode adjoint of n symplectic leap-frog steps for O = Re average_trace_plaquette / 3
+// of the final links.  Pass 1 runs the steps forward from (U0, E0), keeping the state that
+// enters every c-th step; the reverse pass then takes the segments from last to first,
+// recomputes the segment's links U_k and kicked momenta E_k from its checkpoint, and applies
+// the adjoint of each drift and kick (adjoint.cuh).  Device memory: ceil(n/c) checkpoints +
+// c+1 links and c momenta of one segment + the two cotangents; c = ceil(sqrt(n)) by default.
+int lq_leapfrog_adjoint(lq_state *s, double dt, int n_steps, int checkpoint_every, double *objective,
+                        double *d_objective_d_beta, double *grad_links, size_t n_link_doubles, double *grad_efield,
+                        size_t n_efield_doubles, size_t *work_bytes) {
+    LQ_CHECK_STATE(s);
+    if (n_steps <= 0) return LQ_ERR_ZERO_INTEGRATION;
+    if (s->leap) return LQ_ERR_WRONG_STATE_KIND;
+    if (!std::isfinite(dt) || checkpoint_every < 0) return LQ_ERR_INVALID_ARGUMENT;
+    if (grad_links && n_link_doubles != (size_t)s->V * s->dim * 18) return LQ_ERR_INCOMPATIBLE_SIZE;
+    if (grad_efield && n_efield_doubles != (size_t)s->V * s->dim * 8) return LQ_ERR_INCOMPATIBLE_SIZE;
+    State &st = *s;
+    const int n = n_steps;
+    int c = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)n));
+    if (c > n) c = n;
+    const int n_ck = (n + c - 1) / c;
+    const size_t ub = st.link_bytes(), eb = st.efield_bytes();
+    const size_t cu_bytes = st.link_elems() * 2 * st.real_bytes, ce_bytes = st.efield_elems() * st.real_bytes;
+    const size_t total = (size_t)n_ck * (ub + eb) + (size_t)(c + 1) * ub + (size_t)c * eb + cu_bytes + ce_bytes;
+    if (work_bytes) *work_bytes = total;
+    char *arena = nullptr;
+    LQ_CK(cudaMalloc((void **)&arena, total));
+    auto ck_u = [&](int i) { return arena + (size_t)i * (ub + eb); };
+    auto ck_e = [&](int i) { return arena + (size_t)i * (ub + eb) + ub; };
+    char *seg = arena + (size_t)n_ck * (ub + eb);
+    auto seg_u = [&](int j) { return seg + (size_t)j * ub; };
+    auto seg_e = [&](int j) { return seg + (size_t)(c + 1) * ub + (size_t)j * eb; };
+    void *lam_u = seg + (size_t)(c + 1) * ub + (size_t)c * eb;
+    void *lam_e = (char *)lam_u + cu_bytes;
+    const int KD = lq::MD_KICK | lq::MD_DRIFT;
+    const double ce = -std::sqrt(2.0 / 3.0) / st.size; // force coefficient
+    const double kappa = std::sqrt(2.0 * 3.0) / st.size * dt;
+    const double n_plaq = (double)((uint64_t)st.V * (uint64_t)((st.dim * (st.dim - 1)) / 2));
+    int rc = LQ_OK;
+    auto run = [&]() -> int {
+        // pass 1: forward, keeping the state that enters steps 0, c, 2c, ...
+        LQ_CK(cudaMemcpyAsync(seg_u(0), st.U[st.cur], ub, cudaMemcpyDeviceToDevice, st.stream));
+        LQ_CK(cudaMemcpyAsync(seg_e(0), st.E, eb, cudaMemcpyDeviceToDevice, st.stream));
+        int a = 0;
+        for (int k = 0; k < n; ++k) {
+            if (k % c == 0) {
+                LQ_CK(cudaMemcpyAsync(ck_u(k / c), seg_u(a), ub, cudaMemcpyDeviceToDevice, st.stream));
+                LQ_CK(cudaMemcpyAsync(ck_e(k / c), seg_e(0), eb, cudaMemcpyDeviceToDevice, st.stream));
+            }
+            LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, seg_u(a), seg_u(1 - a), seg_e(0), seg_e(0), KD,
+                                                  k == 0 ? 0.0 : dt / 2.0, dt / 2.0, dt));
+            a = 1 - a;
+        }
+        int r = plaquette_sums(st, seg_u(a), 0);
+        if (!r) r = fetch_out(st, 3);
+        if (r) return r;
+        if (objective) *objective = st.h_out[1] / n_plaq / 3.0;
+        // cotangents at the end: lam_U = dO/dU_n, lam_E = 0 (O does not depend on E_n)
+        LQ_LAUNCH(st, LQ_KERNEL_OTHER, st.ops->adj_init(st, seg_u(a), lam_u, 1.0 / (3.0 * n_plaq)));
+        LQ_CK(cudaMemsetAsync(lam_e, 0, ce_bytes, st.stream));
+        for (int sgm = n_ck - 1; sgm >= 0; --sgm) {
+            const int k0 = sgm * c, len = std::min(c, n - k0);
+            // recompute the segment: seg_u(j) = U_{k0+j}, seg_e(j) = momenta after kick k0+j
+            LQ_CK(cudaMemcpyAsync(seg_u(0), ck_u(sgm), ub, cudaMemcpyDeviceToDevice, st.stream));
+            for (int j = 0; j < len; ++j) {
+                const int k = k0 + j;
+                LQ_LAUNCH(st, LQ_KERNEL_MD, st.ops->md(st, seg_u(j), seg_u(j + 1), j == 0 ? ck_e(sgm) : seg_e(j - 1),
+                                                      seg_e(j), KD, k == 0 ? 0.0 : dt / 2.0, dt / 2.0, dt));
+            }
+            for (int j = len - 1; j >= 0; --j) {
+                const int k = k0 + j;
+                LQ_LAUNCH(st, LQ_KERNEL_OTHER, st.ops->adj_drift(st, seg_u(j), seg_e(j), lam_u, lam_e, kappa));
+                const double h = k == 0 ? dt / 2.0 : dt;
+                LQ_LAUNCH(st, LQ_KERNEL_OTHER, st.ops->adj_kick(st, seg_u(j), lam_e, lam_u, h * ce));
+            }
+        }
+        // dO/dbeta for E0(beta) = E0 beta0 / beta: -(1/beta) sum_l,a lam_E^a e0^a
+        uint32_t np = 0;
+        LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->dot(st, lam_e, st.E, &np));
+        LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->finalize(st, 1, np, 0));
+        r = fetch_out(st, 1);
+        if (r) return r;
+        if (d_objective_d_beta) *d_objective_d_beta = -st.h_out[0] / st.beta;
+        if (grad_links) {
+            r = ensure_staging(st, n_link_doubles * sizeof(double));
+            if (r) return r;
+            LQ_LAUNCH(st, LQ_KERNEL_OTHER, st.ops->cot_links_to_aos(st, lam_u, (double *)st.staging));
+            LQ_CK(cudaMemcpyAsync(grad_links, st.staging, n_link_doubles * sizeof(double), cudaMemcpyDeviceToHost,
+                                  st.stream));
+            LQ_CK(sync_stream(st));
+        }
+        if (grad_efield) {
+            r = ensure_staging(st, n_efield_doubles * sizeof(double));
+            if (r) return r;
+            LQ_LAUNCH(st, LQ_KERNEL_OTHER, st.ops->cot_efield_to_aos(st, lam_e, (double *)st.staging));
+            LQ_CK(cudaMemcpyAsync(grad_efield, st.staging, n_efield_doubles * sizeof(double), cudaMemcpyDeviceToHost,
+                                  st.stream));
+            LQ_CK(sync_stream(st));
+        }
+        return LQ_OK;
+    };
+    rc = run();
+    cudaStreamSynchronize(st.stream);
+    cudaFree(arena);
+    return rc;
+}
+
 // ------------------------------------------------------------------ updates
 int lq_project_gauss(lq_state *s, int max_steps, int *steps_done) {
     LQ_CHECK_STATE(s);

@@ -107,6 +107,15 @@ struct Ops {
     cudaError_t (*force)(State &s, const void *U, void *out, double scale);
     // U_mu(site) <- exp(i angle T^a) U_mu(site)
     cudaError_t (*link_rotate)(State &s, void *U, uint32_t site, int mu, int a, double angle);
+    // reverse-mode adjoint of the leap-frog (cotangent arrays hold hi parts only):
+    // lamU <- scale Sigma^dag; lamU += coef d/dU sum Im Tr(W U Sigma); adjoint of one drift
+    cudaError_t (*adj_init)(State &s, const void *U, void *lamU, double scale);
+    cudaError_t (*adj_kick)(State &s, const void *U, const void *lamE, void *lamU, double coef);
+    cudaError_t (*adj_drift)(State &s, const void *U, const void *E, void *lamU, void *lamE, double kappa);
+    // partials of sum a_i b_i over the hi parts of two E-field arrays
+    cudaError_t (*dot)(State &s, const void *a, const void *b, uint32_t *n_partials);
+    cudaError_t (*cot_links_to_aos)(State &s, const void *lamU, double *d_aos);
+    cudaError_t (*cot_efield_to_aos)(State &s, const void *lamE, double *d_aos);
 };
 
 const Ops *ops_f64(int dim);

@@ -33,6 +33,8 @@ PRECISION_MIXED = 1
 PRECISION_F32 = 2
 SYNC_SYNC, SYNC_LEAP, LEAP_LEAP, LEAP_SYNC, SYMPLECTIC, SYMPLECTIC_EXP, SYMPLECTIC_EXP_REUNITARIZE = range(7)
 LINK_UPDATE_EULER, LINK_UPDATE_EXP, LINK_UPDATE_EXP_REUNITARIZE = range(3)
+BATCH_USE_GRAPH, BATCH_MEASURE_PLAQUETTE = 1, 2
+BATCH_KERNEL_CLASSES = ("md", "sweep", "gauss", "plaquette_delta", "sumsq_delta", "normal", "plaquette")
 
 # every symbol the header declares, with (restype, argtypes)
 _vp, _i32, _u64, _f64, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double, ctypes.c_size_t
@@ -76,8 +78,25 @@ SIGNATURES = {
     "lq_wilson_action": (_i32, [_vp, _dp]),
     "lq_wilson_action_backward": (_i32, [_vp, _dp, _sz]),
     "lq_link_rotate": (_i32, [_vp, ctypes.c_longlong, _i32, _f64]),
+    "lq_leapfrog_adjoint": (_i32, [_vp, _f64, _i32, _i32, _dp, _dp, _dp, _sz, _dp, _sz, _szp]),
     "lq_profile_enable": (_i32, [_vp, _i32]),
     "lq_profile_read": (_i32, [_vp, _i32, _llp, _dp, _i32]),
+    "lq_batch_create": (_i32, [_i32, _i32, _ip, _dp, _dp, _i32, ctypes.POINTER(_vp)]),
+    "lq_batch_destroy": (_i32, [_vp]),
+    "lq_batch_set_stream": (_i32, [_vp, _vp]),
+    "lq_batch_info": (_i32, [_vp, _ip, _ip, _llp, _szp]),
+    "lq_batch_set_link_update": (_i32, [_vp, _i32]),
+    "lq_batch_set_seed": (_i32, [_vp, _u64, _u64]),
+    "lq_batch_links_random": (_i32, [_vp, _u64]),
+    "lq_batch_links_upload": (_i32, [_vp, _i32, _dp, _sz]),
+    "lq_batch_links_download": (_i32, [_vp, _i32, _dp, _sz]),
+    "lq_batch_normalize_link_matrices": (_i32, [_vp]),
+    "lq_batch_average_trace_plaquette": (_i32, [_vp, _dp, _dp]),
+    "lq_batch_autotune": (_i32, [_vp, _f64, _i32]),
+    "lq_batch_tuning": (_i32, [_vp, _i32, _ip, _ip, _dp]),
+    "lq_batch_hmc_run": (_i32, [_vp, _f64, _i32, _i32, _i32, _i32]),
+    "lq_batch_hmc_results": (_i32, [_vp, _i32, _i32, _dp, _dp, _dp, _ip, _ip, _ip, _dp]),
+    "lq_batch_graph_launches": (_i32, [_vp, _llp]),
     "lq_status_string": (ctypes.c_char_p, [_i32]),
     "lq_last_error_string": (ctypes.c_char_p, []),
     "lq_version": (_i32, []),
@@ -266,6 +285,22 @@ class State:
         _check(load().lq_link_rotate(self._h, link, generator, angle), "lq_link_rotate")
 
     # ---- updates
+    def leapfrog_adjoint(self, dt, n_steps, checkpoint_every=0, grads=True):
+        """O = <Re Tr P>/3 after n_steps symplectic steps, dO/dbeta (momenta scaled as 1/beta) and,
+        with grads, dO/dU0 (complex cotangent per link, serde layout) and dO/dE0."""
+        o, db, nbytes = ctypes.c_double(), ctypes.c_double(), ctypes.c_size_t()
+        gl = ge = None
+        args = [None, 0, None, 0]
+        if grads:
+            n = self.L ** self.dim * self.dim
+            gl = np.empty((n, 18))
+            ge = np.empty((self.L ** self.dim, self.dim, 8))
+            args = [_p(gl), gl.size, _p(ge), ge.size]
+        _check(load().lq_leapfrog_adjoint(self._h, dt, n_steps, checkpoint_every, ctypes.byref(o), ctypes.byref(db),
+                                          *args, ctypes.byref(nbytes)), "lq_leapfrog_adjoint")
+        return dict(objective=o.value, d_objective_d_beta=db.value, grad_links=gl, grad_efield=ge,
+                    work_bytes=nbytes.value)
+
     def project_to_gauss(self, max_steps=100000):
         steps = ctypes.c_int()
         _check(load().lq_project_gauss(self._h, max_steps, ctypes.byref(steps)), "lq_project_gauss")
@@ -326,3 +361,110 @@ class State:
                                         ctypes.byref(acc), ctypes.byref(p), ctypes.byref(dh), ctypes.byref(steps)),
                "lq_hmc_trajectory")
         return dict(accepted=bool(acc.value), prob=p.value, delta_h=dh.value, gauss_steps=steps.value)
+
+
+class Batch:
+    """Independent HMC ensembles of uneven side length and beta in one set of device arrays
+    (lq_batch_*): every kernel of a trajectory covers all ensembles, and a trajectory can be
+    replayed as one captured CUDA graph."""
+
+    def __init__(self, dim, Ls, sizes, betas, precision=PRECISION_MIXED):
+        lib = load()
+        n = len(Ls)
+        if len(sizes) != n or len(betas) != n:
+            raise ValueError("Ls, sizes and betas must have the same length")
+        self.Ls = np.ascontiguousarray(Ls, dtype=np.int32)
+        sz = np.ascontiguousarray(sizes, dtype=np.float64)
+        bt = np.ascontiguousarray(betas, dtype=np.float64)
+        h = _vp()
+        _check(lib.lq_batch_create(dim, n, self.Ls.ctypes.data_as(_ip), _p(sz), _p(bt), precision, ctypes.byref(h)),
+               "lq_batch_create")
+        self._h = h
+        self.dim, self.n, self.precision = dim, n, precision
+        self.sizes, self.betas = sz, bt
+        self.last_run = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().lq_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_ptr):
+        _check(load().lq_batch_set_stream(self._h, _vp(stream_ptr)), "lq_batch_set_stream")
+
+    def info(self):
+        d, n, links, nbytes = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong(), ctypes.c_size_t()
+        _check(load().lq_batch_info(self._h, ctypes.byref(d), ctypes.byref(n), ctypes.byref(links),
+                                    ctypes.byref(nbytes)), "lq_batch_info")
+        return dict(dim=d.value, n_ensembles=n.value, total_links=links.value, device_bytes=nbytes.value)
+
+    def set_link_update(self, link_update):
+        _check(load().lq_batch_set_link_update(self._h, link_update), "lq_batch_set_link_update")
+
+    def set_seed(self, seed, counter=0):
+        _check(load().lq_batch_set_seed(self._h, seed, counter), "lq_batch_set_seed")
+
+    def set_links_random(self, seed):
+        _check(load().lq_batch_links_random(self._h, seed), "lq_batch_links_random")
+
+    def set_link_matrix(self, e, links):
+        a = np.ascontiguousarray(links, dtype=np.float64)
+        _check(load().lq_batch_links_upload(self._h, e, _p(a), a.size), "lq_batch_links_upload")
+
+    def link_matrix(self, e):
+        out = np.empty((int(self.Ls[e]) ** self.dim * self.dim, 18), dtype=np.float64)
+        _check(load().lq_batch_links_download(self._h, e, _p(out), out.size), "lq_batch_links_download")
+        return out
+
+    def normalize_link_matrices(self):
+        _check(load().lq_batch_normalize_link_matrices(self._h), "lq_batch_normalize_link_matrices")
+
+    def average_trace_plaquette(self):
+        re, im = np.empty(self.n), np.empty(self.n)
+        _check(load().lq_batch_average_trace_plaquette(self._h, _p(re), _p(im)), "lq_batch_average_trace_plaquette")
+        return re + 1j * im
+
+    def autotune(self, dt=0.01, reps=3):
+        _check(load().lq_batch_autotune(self._h, dt, reps), "lq_batch_autotune")
+        return self.tuning()
+
+    def tuning(self):
+        out = {}
+        for cls, name in enumerate(BATCH_KERNEL_CLASSES):
+            g, o, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+            _check(load().lq_batch_tuning(self._h, cls, ctypes.byref(g), ctypes.byref(o), ctypes.byref(ms)),
+                   "lq_batch_tuning")
+            out[name] = dict(grid=g.value, order=o.value, ms=ms.value)
+        return out
+
+    def hmc_run(self, dt, n_steps, n_trajectories, max_gauss_steps=0, graph=True, measure_plaquette=False):
+        flags = (BATCH_USE_GRAPH if graph else 0) | (BATCH_MEASURE_PLAQUETTE if measure_plaquette else 0)
+        _check(load().lq_batch_hmc_run(self._h, dt, n_steps, n_trajectories, max_gauss_steps, flags),
+               "lq_batch_hmc_run")
+        self.last_run = n_trajectories
+
+    def hmc_results(self, first=0, count=None):
+        """Per-trajectory, per-ensemble results of the last run, arrays [count, n_ensembles]."""
+        count = self.last_run - first if count is None else count
+        shape = (count, self.n)
+        dh, p, u, pl = (np.empty(shape) for _ in range(4))
+        acc, steps, st = (np.empty(shape, dtype=np.int32) for _ in range(3))
+        ip = lambda a: a.ctypes.data_as(_ip)
+        _check(load().lq_batch_hmc_results(self._h, first, count, _p(dh), _p(p), _p(u), ip(acc), ip(steps), ip(st),
+                                           _p(pl)), "lq_batch_hmc_results")
+        return dict(delta_h=dh, prob=p, uniform=u, accepted=acc.astype(bool), gauss_steps=steps, status=st,
+                    plaquette=pl)
+
+    def graph_launches(self):
+        n = ctypes.c_longlong()
+        _check(load().lq_batch_graph_launches(self._h, ctypes.byref(n)), "lq_batch_graph_launches")
+        return n.value

@@ -8,12 +8,21 @@ precision : D = 4, 32^4, beta in {0.5, 1, 2, 4}, random_su3 start (seed 1), 20 l
             through lq_hmc_refresh_upload) and accept uniforms; reported per beta: max |Delta H
             error|, max |Delta <P>/3|, acceptance of each form, and the forward/backward
             reversibility of one trajectory (momenta flipped at the end, integrated back).
-            Mixed reprojects its links (FP64) every 10 trajectories.
+            Mixed reprojects its links (FP64) every 10 trajectories.  Where the Gauss projection
+            of the momenta fails (the reference's relaxation diverges to NaN for momentum
+            standard deviations near 1, i.e. beta = 0.5), the beta records the failure.
 scale     : D = 4 at 24^4, 32^4, 48^4, 64^4 and D = 3 at 128^3, 256^3, beta 2, seed 4, 20 steps
             dt 0.005: link-updates/s of FP64 and mixed (device time of K trajectories), the
             k_md kernel's achieved HBM bandwidth, and the Delta H / plaquette error of mixed.
 
-usage: python studies.py precision [--traj N] | scale [--traj K]
+batch     : 64 ensembles of uneven side length and beta advanced together (one launch per kernel
+            over every ensemble, a CUDA graph per trajectory), against the same ensembles run
+            one after another as single states.
+
+adjoint   : d<plaq>/dbeta through a 50-step leap-frog at 48^4 by the checkpointed reverse-mode
+            adjoint, FP32 and FP64, each against its central difference in beta.
+
+usage: python studies.py precision [--traj N] | scale [--traj K] | batch [--traj N] | adjoint [--L 48]
 """
 import argparse
 import json
@@ -57,12 +66,18 @@ def precision_study(args):
         err_pl = {p: 0.0 for p in forms[1:]}
         dh_ref = []
         t0 = time.time()
+        failure = None
         for k in range(args.traj):
             e_raw = rng.normal(0.0, 0.5 / beta, size=(L ** dim, dim, 8))
             u = float(rng.uniform())
             res = {}
             for p, s in states.items():
-                s.hmc_refresh_upload(e_raw)
+                try:
+                    s.hmc_refresh_upload(e_raw)
+                except lqgpu.LqError as err:
+                    # the reference's projection (K = 0.12 relaxation) diverges for large momenta
+                    failure = {"trajectory": k, "form": PREC_NAMES[p], "error": str(err)}
+                    break
                 prob, h0, h1 = s.hmc_propose(dt, nmd)
                 a = prob >= 1.0 or u < prob
                 s.hmc_decide(a)
@@ -70,10 +85,19 @@ def precision_study(args):
                 res[p] = (h1 - h0, s.average_trace_plaquette().real / 3.0)
                 if p == lqgpu.PRECISION_MIXED and (k + 1) % 10 == 0:
                     s.normalize_link_matrices()
+            if failure:
+                break
             dh_ref.append(res[lqgpu.PRECISION_F64][0])
             for p in forms[1:]:
                 err_dh[p] = max(err_dh[p], abs(res[p][0] - res[lqgpu.PRECISION_F64][0]))
                 err_pl[p] = max(err_pl[p], abs(res[p][1] - res[lqgpu.PRECISION_F64][1]))
+        if failure:
+            out["betas"][str(beta)] = {"seconds": round(time.time() - t0, 1), "momentum_std_dev": 0.5 / beta,
+                                       "gauss_projection_failed": failure}
+            for s in states.values():
+                s.close()
+            print(json.dumps({"beta": beta, **out["betas"][str(beta)]}), flush=True)
+            continue
         # forward/backward reversibility of one trajectory of each form
         rev = {}
         for p, s in states.items():
@@ -165,9 +189,133 @@ def scale_study(args):
     return out
 
 
+def batch_study(args):
+    """64 independent ensembles, D = 4, side lengths drawn from {8, 10, 12, 16, 20} (seed 3),
+    beta linearly spaced 0.5 .. 3.5, random_su3 starts, mixed form, 10 leap-frog steps
+    dt 0.01, N trajectories each: batched (one launch per kernel over every ensemble, one graph
+    launch per trajectory, autotuned launch shapes) against the same ensembles run one after
+    another as single states (two trajectories each, scaled)."""
+    import torch
+
+    n_ens, dt, nmd, size = 64, 0.01, 10, 1000.0
+    Ls = np.random.default_rng(3).choice([8, 10, 12, 16, 20], size=n_ens)
+    betas = np.linspace(0.5, 3.5, n_ens)
+    peak = hbm_peak()
+    b = lqgpu.Batch(4, Ls, [size] * n_ens, betas, lqgpu.PRECISION_MIXED)
+    info = b.info()
+    b.set_links_random(3)
+    b.set_seed(3, 0)
+    t0 = time.time()
+    tuning = b.autotune(dt, 3)
+    tune_s = time.time() - t0
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    b.hmc_run(dt, nmd, 2)  # capture + warm-up
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    w0 = time.time()
+    e0.record(stream)
+    b.hmc_run(dt, nmd, args.traj, measure_plaquette=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.time() - w0
+    ms = e0.elapsed_time(e1)
+    r = b.hmc_results()
+    links = info["total_links"]
+    md_ms = tuning["md"]["ms"]
+    md_bytes = links * 4 * 52 * 2  # compensated FP32: 52 reals of (hi, lo) per link
+    ok = r["status"] == 0
+    out = {"study": "batch", "ensembles": n_ens, "dim": 4, "L_counts": {int(L): int((Ls == L).sum()) for L in (8, 10, 12, 16, 20)},
+           "beta": [0.5, 3.5], "dt": dt, "md_steps": nmd, "trajectories": args.traj, "total_links": links,
+           "device_bytes": info["device_bytes"], "autotune_seconds": round(tune_s, 2), "tuning": tuning,
+           "ms_per_trajectory": ms / args.traj, "wall_s": wall,
+           "link_updates_per_s": links * nmd * args.traj / (ms / 1e3),
+           "md_launch_ms": md_ms, "md_hbm_gbs": md_bytes / (md_ms / 1e3) / 1e9,
+           "md_hbm_frac": md_bytes / (md_ms / 1e3) / 1e9 / peak,
+           "graph_launches": b.graph_launches(),
+           "projection_failures": int((~ok).sum()),
+           "failed_ensembles_beta": sorted(set(float(round(betas[e], 3)) for e in np.nonzero(~ok.all(axis=0))[0])),
+           "acceptance_mean": float(r["accepted"][ok].mean()) if ok.any() else None,
+           "max_abs_delta_h": float(np.abs(r["delta_h"][ok]).max()) if ok.any() else None,
+           "gauss_steps_range": [int(r["gauss_steps"][ok].min()), int(r["gauss_steps"][ok].max())] if ok.any() else None}
+    b.close()
+    # the same ensembles one after another (the reference's way of scanning), 2 trajectories each
+    seq_ms, seq_links = 0.0, 0
+    for e in range(n_ens):
+        s = lqgpu.State(4, int(Ls[e]), size, float(betas[e]), lqgpu.PRECISION_MIXED)
+        s.set_links_random(3 + e)
+        s.set_stream(stream.cuda_stream)
+        try:
+            s.hmc_trajectory(dt, nmd, 3 + e, 0, 0.5)
+        except lqgpu.LqError:
+            pass
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(2):
+            try:
+                s.hmc_trajectory(dt, nmd, 3 + e, 1 + k, 0.5)
+            except lqgpu.LqError:
+                pass
+        e1.record(stream)
+        torch.cuda.synchronize()
+        seq_ms += e0.elapsed_time(e1)
+        seq_links += int(Ls[e]) ** 4 * 4 * nmd * 2
+        s.close()
+    out["sequential_link_updates_per_s"] = seq_links / (seq_ms / 1e3)
+    out["batched_over_sequential"] = out["link_updates_per_s"] / out["sequential_link_updates_per_s"]
+    print(json.dumps(out), flush=True)
+    return out
+
+
+def adjoint_study(args):
+    """d<plaq>/dbeta through a 50-step dt 0.01 leap-frog by the reverse-mode adjoint with
+    sqrt(n) checkpointing: D = 4, 48^4, beta 2, size 1, random links (seed 2), momenta
+    N(0, 0.5/beta) (numpy seed 2); the FP32 form against the FP64 form and against the
+    central difference in beta (delta beta 1e-4) of each form."""
+    import torch
+
+    dim, L, beta, size, dt, n, db = 4, args.L, 2.0, 1.0, 0.01, 50, 1e-4
+    e_raw = np.random.default_rng(2).normal(0.0, 0.5 / beta, size=(L ** dim, dim, 8))
+    out = {"study": "adjoint", "dim": dim, "L": L, "beta": beta, "size": size, "dt": dt, "steps": n, "forms": {}}
+    for p in (lqgpu.PRECISION_F32, lqgpu.PRECISION_F64):
+        s = lqgpu.State(dim, L, size, beta, p)
+        s.set_links_random(2)
+        s.set_e_field(e_raw)
+        links, e0 = s.link_matrix(), s.e_field()
+        torch.cuda.synchronize()
+        t0 = time.time()
+        r = s.leapfrog_adjoint(dt, n, grads=False)
+        t_adj = time.time() - t0
+
+        def objective(e):
+            s.set_link_matrix(links)
+            s.set_e_field(e)
+            s.integrate(lqgpu.SYMPLECTIC, dt, n)
+            return s.average_trace_plaquette().real / 3.0
+
+        t0 = time.time()
+        fd = (objective(e0 * beta / (beta + db)) - objective(e0 * beta / (beta - db))) / (2 * db)
+        t_fd = time.time() - t0
+        state_bytes = s.device_bytes()
+        n_ck = -(-n // int(np.ceil(np.sqrt(n))))
+        one = (L ** dim * dim) * (18 + 8) * (8 if p == lqgpu.PRECISION_F64 else 4)
+        out["forms"][PREC_NAMES[p]] = {
+            "objective": r["objective"], "d_objective_d_beta": r["d_objective_d_beta"],
+            "central_difference": fd, "relative_difference_to_fd": abs(r["d_objective_d_beta"] - fd) / abs(fd),
+            "adjoint_seconds": round(t_adj, 2), "fd_seconds_two_trajectories": round(t_fd, 2),
+            "work_bytes_checkpointed": r["work_bytes"], "checkpoints": n_ck,
+            "work_bytes_all_steps_stored": (n + 1) * one, "state_bytes": state_bytes}
+        s.close()
+        print(json.dumps({PREC_NAMES[p]: out["forms"][PREC_NAMES[p]]}), flush=True)
+    f32, f64 = out["forms"]["f32"], out["forms"]["f64"]
+    out["f32_vs_f64_relative"] = abs(f32["d_objective_d_beta"] - f64["d_objective_d_beta"]) / abs(f64["d_objective_d_beta"])
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "scale"])
+    ap.add_argument("study", choices=["precision", "scale", "batch", "adjoint"])
     ap.add_argument("--traj", type=int, default=None)
     ap.add_argument("--L", type=int, default=32)
     ap.add_argument("--betas", type=float, nargs="*", default=[0.5, 1.0, 2.0, 4.0])
@@ -175,9 +323,16 @@ def main():
     if args.study == "precision":
         args.traj = args.traj or 100
         res = precision_study(args)
-    else:
+    elif args.study == "scale":
         args.traj = args.traj or 10
         res = scale_study(args)
+    elif args.study == "batch":
+        args.traj = args.traj or 50
+        res = batch_study(args)
+    else:
+        if args.L == 32:
+            args.L = 48
+        res = adjoint_study(args)
     print(json.dumps(res))
 
 

@@ -76,3 +76,30 @@ def test_no_cpu_fallback_without_device(lqgpu_mod):
     assert rc == lqgpu_mod.LQ_ERR_NO_DEVICE
     with pytest.raises(lqgpu_mod.LqError):
         lqgpu_mod.State(2, 4)
+
+
+def test_batch_argument_validation_precedes_device_use(lqgpu_mod):
+    """lq_batch_create checks every ensemble as lq_state_create checks one lattice (plus the
+    momentum distribution N(0, 0.5/beta) per ensemble) before any device call."""
+    G = lqgpu_mod
+    lib = G.load()
+    h = ctypes.c_void_p()
+
+    def create(dim, Ls, sizes, betas, precision=1):
+        n = len(Ls)
+        L = (ctypes.c_int * n)(*Ls)
+        sz = (ctypes.c_double * n)(*sizes)
+        bt = (ctypes.c_double * n)(*betas)
+        return lib.lq_batch_create(dim, n, ctypes.cast(L, G._ip), ctypes.cast(sz, G._dp), ctypes.cast(bt, G._dp),
+                                   precision, ctypes.byref(h))
+
+    assert create(0, [4, 4], [1.0, 1.0], [1.0, 1.0]) == G.LQ_ERR_ZERO_DIMENSION
+    assert create(4, [4, 4], [1.0, 0.0], [1.0, 1.0]) == G.LQ_ERR_NON_POSITIVE_SIZE
+    assert create(4, [4, 1], [1.0, 1.0], [1.0, 1.0]) == G.LQ_ERR_DIM_TOO_SMALL
+    assert create(5, [4, 4], [1.0, 1.0], [1.0, 1.0]) == G.LQ_ERR_UNSUPPORTED_DIM
+    assert create(4, [4, 4], [1.0, 1.0], [1.0, 0.0]) == G.LQ_ERR_INVALID_NORMAL
+    assert create(4, [4, 4], [1.0, 1.0], [1.0, -1.0]) == G.LQ_ERR_INVALID_NORMAL
+    assert create(4, [4, 4], [1.0, 1.0], [1.0, 1.0], precision=7) == G.LQ_ERR_INVALID_ARGUMENT
+    assert lib.lq_batch_create(4, 0, None, None, None, 1, ctypes.byref(h)) == G.LQ_ERR_INVALID_ARGUMENT
+    assert lib.lq_batch_hmc_run(None, 0.1, 1, 1, 0, 1) == G.LQ_ERR_INVALID_ARGUMENT
+    assert lib.lq_batch_destroy(None) == G.LQ_OK

@@ -1,0 +1,144 @@
+"""Batched ensembles (lq_batch_*): many lattices of uneven side length and beta advanced by
+one launch per kernel of a trajectory, replayed as a CUDA graph with the Gauss projection's
+sweep loop as a device-side while node.
+
+Each ensemble of a batch must evolve exactly as a state of the same precision run alone
+through lq_hmc_trajectory with the same seed (batch seed + ensemble index), counter and
+accept uniform: the per-link arithmetic is shared, so the links after K trajectories are
+bitwise equal for the FP32-arithmetic forms (both use the fused projection sweep) and equal
+to 1e-12 for FP64 (the state projects with two kernels per step, the batch with the fused
+sweep).  Delta H is compared to 1e-9 relative to the link Hamiltonian: the state forms it
+as a difference of two Hamiltonians (FP64) or of Hamiltonian updates, the batch from the
+difference kernels directly."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DIM = 4
+LS = [3, 4, 5, 4, 3]
+BETAS = [1.5, 2.0, 3.0, 2.5, 6.0]
+SIZES = [1000.0, 1000.0, 1000.0, 20.0, 1000.0]
+SEED, LINK_SEED = 77, 5
+DT, NSTEPS, NTRAJ, MAXG = 0.01, 6, 4, 10001
+
+
+def make_batch(G, precision, Ls=LS, betas=BETAS, sizes=SIZES):
+    b = G.Batch(DIM, Ls, sizes, betas, precision)
+    b.set_links_random(LINK_SEED)
+    b.set_seed(SEED, 0)
+    return b
+
+
+@pytest.mark.parametrize("precision", [1, 2, 0])
+def test_batch_matches_single_lattice_runs(lqgpu_mod, precision):
+    G = lqgpu_mod
+    with make_batch(G, precision) as b:
+        b.hmc_run(DT, NSTEPS, NTRAJ, MAXG, graph=True)
+        res = b.hmc_results()
+        links_b = [b.link_matrix(e) for e in range(b.n)]
+    assert (res["status"] == 0).all()
+    for e, (L, beta, size) in enumerate(zip(LS, BETAS, SIZES)):
+        with G.State(DIM, L, size, beta, precision) as s:
+            s.set_links_random(LINK_SEED + e)
+            hu = s.hamiltonian_links()
+            for k in range(NTRAJ):
+                r = s.hmc_trajectory(DT, NSTEPS, SEED + e, k, float(res["uniform"][k, e]), MAXG)
+                assert r["gauss_steps"] == res["gauss_steps"][k, e]
+                assert r["accepted"] == res["accepted"][k, e]
+                assert abs(r["delta_h"] - res["delta_h"][k, e]) <= 1e-9 * max(1.0, hu)
+            if precision == 0:
+                assert np.abs(s.link_matrix() - links_b[e]).max() <= 1e-12
+            else:
+                assert np.array_equal(s.link_matrix(), links_b[e])
+
+
+def test_graph_replay_equals_eager_launches(lqgpu_mod):
+    G = lqgpu_mod
+    out = []
+    for graph in (True, False):
+        with make_batch(G, G.PRECISION_MIXED) as b:
+            b.hmc_run(DT, NSTEPS, NTRAJ, MAXG, graph=graph, measure_plaquette=True)
+            out.append((b.hmc_results(), [b.link_matrix(e) for e in range(b.n)], b.graph_launches()))
+    (ra, la, na), (rb, lb, nb) = out
+    assert na == NTRAJ and nb == 0
+    for key in ("delta_h", "accepted", "gauss_steps", "uniform", "plaquette"):
+        assert np.array_equal(ra[key], rb[key]), key
+    for x, y in zip(la, lb):
+        assert np.array_equal(x, y)
+
+
+def test_results_do_not_depend_on_tuned_launch_shapes(lqgpu_mod):
+    G = lqgpu_mod
+    runs = []
+    for tune in (False, True):
+        with make_batch(G, G.PRECISION_MIXED) as b:
+            if tune:
+                t = b.autotune(DT, 2)
+                assert all(v["ms"] > 0.0 for v in t.values())
+            b.hmc_run(DT, NSTEPS, 2, MAXG)
+            runs.append((b.hmc_results(), [b.link_matrix(e) for e in range(b.n)]))
+    assert np.array_equal(runs[0][0]["delta_h"], runs[1][0]["delta_h"])
+    for x, y in zip(runs[0][1], runs[1][1]):
+        assert np.array_equal(x, y)
+
+
+def test_persistent_grids_give_the_same_links(lqgpu_mod):
+    """Tuning picks grids of a few waves for the larger batch; links equal the untuned run."""
+    G = lqgpu_mod
+    Ls, betas, sizes = [6, 8, 7, 5, 8, 6], [2.0, 2.5, 3.0, 1.5, 4.0, 2.2], [1000.0] * 6
+    runs = []
+    for tune in (False, True):
+        with make_batch(G, G.PRECISION_F32, Ls, betas, sizes) as b:
+            if tune:
+                b.autotune(DT, 1)
+            b.hmc_run(DT, 3, 2, MAXG)
+            runs.append([b.link_matrix(e) for e in range(b.n)])
+    for x, y in zip(*runs):
+        assert np.array_equal(x, y)
+
+
+def test_step_limit_keeps_links_and_reports_status(lqgpu_mod):
+    G = lqgpu_mod
+    with make_batch(G, G.PRECISION_MIXED) as b:
+        before = [b.link_matrix(e) for e in range(b.n)]
+        b.hmc_run(DT, NSTEPS, 2, max_gauss_steps=2)
+        r = b.hmc_results()
+        after = [b.link_matrix(e) for e in range(b.n)]
+    # a random draw is not projected after one step: every ensemble stops at the limit
+    assert (r["status"] == G.LQ_ERR_NOT_CONVERGED).all()
+    assert not r["accepted"].any()
+    for x, y in zip(before, after):
+        assert np.array_equal(x, y)
+
+
+def test_recorded_plaquette_and_batch_observables(lqgpu_mod):
+    G = lqgpu_mod
+    with make_batch(G, G.PRECISION_MIXED) as b:
+        b.hmc_run(DT, NSTEPS, 3, MAXG, measure_plaquette=True)
+        r = b.hmc_results()
+        plaq = b.average_trace_plaquette()
+        links = [b.link_matrix(e) for e in range(b.n)]
+    assert np.array_equal(r["plaquette"][-1], plaq.real)
+    for e, (L, beta, size) in enumerate(zip(LS, BETAS, SIZES)):
+        with G.State(DIM, L, size, beta, G.PRECISION_F64) as s:
+            s.set_link_matrix(links[e])
+            assert abs(s.average_trace_plaquette() - plaq[e]) <= 1e-6
+
+
+def test_uneven_batch_dims_2_and_3(lqgpu_mod):
+    G = lqgpu_mod
+    for dim, Ls in ((2, [5, 9, 4]), (3, [3, 6, 4])):
+        with G.Batch(dim, Ls, [1000.0] * 3, [2.0, 3.0, 4.0], G.PRECISION_MIXED) as b:
+            b.set_links_random(3)
+            b.set_seed(11, 0)
+            b.hmc_run(0.02, 4, 2, MAXG)
+            res = b.hmc_results()
+            links = [b.link_matrix(e) for e in range(3)]
+        for e, L in enumerate(Ls):
+            with G.State(dim, L, 1000.0, [2.0, 3.0, 4.0][e], G.PRECISION_MIXED) as s:
+                s.set_links_random(3 + e)
+                for k in range(2):
+                    r = s.hmc_trajectory(0.02, 4, 11 + e, k, float(res["uniform"][k, e]), MAXG)
+                    assert r["accepted"] == res["accepted"][k, e]
+                assert np.array_equal(s.link_matrix(), links[e])

@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--batch-traj", type=int, default=10,
+                    help="timed trajectories of the batched-ensembles leg (0: skip it)")
     return ap.parse_args()
 
 
@@ -241,6 +243,49 @@ def replica_value(units, ms, max_over_ranks, sum_over_ranks):
     return sum_over_ranks(units) / (max_over_ranks(ms) / 1000.0)
 
 
+def batch_leg(args, stream, peak):
+    """The parameter-scan workload: 64 ensembles, D = 4, side lengths drawn from {8, 10, 12, 16, 20}
+    (seed 3), beta linearly spaced 0.5 .. 3.5, size 1000, mixed, 10 leap-frog steps dt 0.01; every
+    kernel one launch over all ensembles, one CUDA-graph launch per trajectory, autotuned shapes."""
+    import numpy as np
+    import torch
+
+    import lqgpu
+
+    n_ens, dt, nmd = 64, 0.01, 10
+    Ls = np.random.default_rng(3).choice([8, 10, 12, 16, 20], size=n_ens)
+    betas = np.linspace(0.5, 3.5, n_ens)
+    b = lqgpu.Batch(4, Ls, [1000.0] * n_ens, betas, lqgpu.PRECISION_MIXED)
+    links = b.info()["total_links"]
+    b.set_links_random(3)
+    b.set_seed(3, 0)
+    tuning = b.autotune(dt, 3)
+    b.set_stream(stream.cuda_stream)
+    b.hmc_run(dt, nmd, 3)  # graph capture + warm-up
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = b.graph_launches()
+    ev0.record(stream)
+    b.hmc_run(dt, nmd, args.batch_traj)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    r = b.hmc_results()
+    launches = b.graph_launches() - launches0
+    b.close()
+    md_bytes = links * 52 * 8
+    ok = r["status"] == 0
+    return {"workload": "64 ensembles D=4, L from {8,10,12,16,20} (seed 3), beta 0.5..3.5, size 1000, mixed, "
+                        "10 leap-frog steps dt 0.01; one launch per kernel over all ensembles, one CUDA graph "
+                        "per trajectory", "total_links": links, "trajectories": args.batch_traj,
+            "value": links * nmd * args.batch_traj / (ms / 1000.0), "unit": UNIT,
+            "ms_per_trajectory": ms / args.batch_traj, "graph_launches": launches, "md_launch_ms": tuning["md"]["ms"],
+            "md_hbm_frac": md_bytes / (tuning["md"]["ms"] / 1000.0) / 1e9 / peak,
+            "tuning": {k: [v["grid"], v["order"]] for k, v in tuning.items()},
+            "projection_failures": int((~ok).sum()),
+            "acceptance": float(r["accepted"][ok].mean()) if ok.any() else None}
+
+
 def run_ours(args):
     rank, world, local_rank = dist_env()
     if world > 1:
@@ -401,6 +446,8 @@ def run_ours(args):
         so.close()
         s64.close()
 
+    batch = batch_leg(args, stream, peak) if args.batch_traj > 0 else None
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, threads, n, t = cpu_trajectory_rate(dim, args.cpu_sample_L, beta, dt, nmd, size, args.cpu_seconds)
@@ -433,7 +480,7 @@ def run_ours(args):
             "gauss_steps": gauss_steps, "acceptance": acc_rate, "plaquette": plaq_mixed.real / 3.0,
             "wall_ms_per_step": 1000.0 * wall / args.steps,
             "clocks": clocks, "e2e": e2e, "fp64": fp64, "other_precision": f32, "accuracy": accuracy,
-            "cpu_baseline": cpu,
+            "batch": batch, "cpu_baseline": cpu,
         }
         print(json.dumps(line))
     if pg is not None:

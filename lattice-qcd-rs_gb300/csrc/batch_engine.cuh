@@ -28,6 +28,14 @@ template <typename T> struct BView {
     uint32_t n_chunks;
 };
 
+// buffer selection by value: indexing the kernel-parameter arrays with a runtime index would
+// copy the whole view to local memory
+template <typename T> __device__ __forceinline__ V2<T> *sel_u(const BView<T> &v, int r) {
+    return r == 0 ? v.U[0] : (r == 1 ? v.U[1] : v.U[2]);
+}
+template <typename T> __device__ __forceinline__ T *sel_e(const BView<T> &v, int r) { return r == 0 ? v.E[0] : v.E[1]; }
+template <typename T> __device__ __forceinline__ T *sel_g(const BView<T> &v, int r) { return r == 0 ? v.G[0] : v.G[1]; }
+
 template <int D> __device__ __forceinline__ Geo<D> geo_of(const BatchEns &e) {
     Geo<D> g;
     g.V = e.V;
@@ -74,7 +82,7 @@ __global__ void __launch_bounds__(128) k_normal_batch(BView<T> v, int eout, int 
         if (site >= en.V) continue;
         const unsigned long long ctr = v.run[c.x].counter;
         const size_t eb = (size_t)en.tile0 * (D * 8 * kTile);
-        efield_normal_link<D, T, COMP>(v.E[eout] + eb, site, mu, key_of(v.keys[c.x]), (uint32_t)ctr,
+        efield_normal_link<D, T, COMP>(sel_e(v, eout) + eb, site, mu, key_of(v.keys[c.x]), (uint32_t)ctr,
                                        (uint32_t)(ctr >> 32), (T)(0.5 / en.beta), v.elo);
     }
 }
@@ -90,7 +98,7 @@ __global__ void __launch_bounds__(128) k_gauss_batch(BView<T> v, int ein, int go
         const int cur = v.run[c.x].cur;
         const size_t ub = (size_t)en.tile0 * (D * 9 * kTile), eb = (size_t)en.tile0 * (D * 8 * kTile),
                      gb = (size_t)en.tile0 * (9 * kTile);
-        (void)gauss_site<D, T>(v.U[cur] + ub, v.E[ein] + eb, v.G[gout] + gb, geo_of<D>(en), site);
+        (void)gauss_site<D, T>(sel_u(v, cur) + ub, sel_e(v, ein) + eb, sel_g(v, gout) + gb, geo_of<D>(en), site);
     }
 }
 
@@ -109,8 +117,8 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_sweep_batch(BView<
             const int cur = v.run[c.x].cur;
             const size_t ub = (size_t)en.tile0 * (D * 9 * kTile), eb = (size_t)en.tile0 * (D * 8 * kTile),
                          gb = (size_t)en.tile0 * (9 * kTile);
-            r[0] = sweep_site<D, T, false>(v.U[cur] + ub, v.E[ein] + eb, v.E[eout] + eb, v.G[gin] + gb,
-                                           v.G[gout] + gb, geo_of<D>(en), site, v.elo);
+            r[0] = sweep_site<D, T, false>(sel_u(v, cur) + ub, sel_e(v, ein) + eb, sel_e(v, eout) + eb, sel_g(v, gin) + gb,
+                                           sel_g(v, gout) + gb, geo_of<D>(en), site, v.elo);
         }
         block_reduce_store<1>(r, v.partial, chunk, v.n_chunks);
         __syncthreads();
@@ -183,8 +191,8 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md_batch(BView<T> v, 
         // the single-lattice coefficients (Engine::md), per ensemble
         const double ce = -sqrt(2.0 / 3.0) / en.size;
         const double cu = sqrt(2.0 * 3.0) / en.size * dt;
-        md_link<D, T, COMP, MODE>(v.U[(cur + rin) % 3] + ub, v.U[(cur + rout) % 3] + ub, v.E[ein] + eb,
-                                  v.E[eout] + eb, geo_of<D>(en), site, mu, (T)(h1 * ce), (T)(h2 * ce), (T)cu,
+        md_link<D, T, COMP, MODE>(sel_u(v, (cur + rin) % 3) + ub, sel_u(v, (cur + rout) % 3) + ub, sel_e(v, ein) + eb,
+                                  sel_e(v, eout) + eb, geo_of<D>(en), site, mu, (T)(h1 * ce), (T)(h2 * ce), (T)cu,
                                   v.ulo, v.elo);
     }
 }
@@ -200,7 +208,7 @@ __global__ void __launch_bounds__(128) k_plaquette_delta_batch(BView<T> v, int r
         if (site < en.V) {
             const int cur = v.run[c.x].cur;
             const size_t ub = (size_t)en.tile0 * (D * 9 * kTile);
-            r[0] = plaquette_delta_site<D, T, COMP>(v.U[(cur + r_old) % 3] + ub, v.U[(cur + r_new) % 3] + ub,
+            r[0] = plaquette_delta_site<D, T, COMP>(sel_u(v, (cur + r_old) % 3) + ub, sel_u(v, (cur + r_new) % 3) + ub,
                                                     geo_of<D>(en), site, v.ulo);
         }
         block_reduce_store<1>(r, v.partial, chunk, v.n_chunks);
@@ -218,8 +226,8 @@ __global__ void __launch_bounds__(128) k_sumsq_delta_batch(BView<T> v, int e_old
         T acc = T(0);
         if (site < en.V) {
             const size_t eb = (size_t)en.tile0 * (D * 8 * kTile);
-            const T *eo = v.E[e_old] + eb;
-            const T *ew = v.E[e_new] + eb;
+            const T *eo = sel_e(v, e_old) + eb;
+            const T *ew = sel_e(v, e_new) + eb;
 #pragma unroll 8
             for (int p = 0; p < D * 8; ++p) {
                 const size_t i = tix(site, D * 8, p);
@@ -245,7 +253,7 @@ __global__ void __launch_bounds__(128) k_plaquette_batch(BView<T> v, int role) {
         double r[3] = {0.0, 0.0, 0.0};
         if (site < en.V) {
             const int cur = v.run[c.x].cur;
-            plaquette_site<D, T>(v.U[(cur + role) % 3] + (size_t)en.tile0 * (D * 9 * kTile), geo_of<D>(en), site,
+            plaquette_site<D, T>(sel_u(v, (cur + role) % 3) + (size_t)en.tile0 * (D * 9 * kTile), geo_of<D>(en), site,
                                  r);
         }
         block_reduce_store<3>(r, v.partial, chunk, v.n_chunks);

@@ -23,11 +23,24 @@ namespace lq {
 
 constexpr uint32_t kChunk = 128; // sites per chunk = threads per block of the batched kernels
 
+// rows of n_chunks partials: the plaquette difference keeps D (D - 1) / 2 (one per plane), the
+// E-field difference one more; the sweep residuals and plaquette sums use up to three
+inline size_t batch_partial_rows(int dim) {
+    const int np = dim * (dim - 1) / 2;
+    return (size_t)(np + 1 > 3 ? np + 1 : 3);
+}
+
 // per ensemble, constant after creation (device copy)
 struct BatchEns {
     uint32_t V, L, tile0, chunk0, nchunks, pad;
     uint32_t stride[4];
     double size, beta;
+    // coefficients in the single-lattice path's arithmetic (Engine::md, Engine::efield_normal),
+    // computed on the host in double and stored in both storage types so that no kernel needs
+    // FP64 arithmetic per work item: momentum std dev 0.5 / beta, half kick (dt/2) c_e with
+    // c_e = -sqrt(2/3) / size, drift dt sqrt(6) / size (kh, dr follow the dt of the last run)
+    double sd_d, kh_d, dr_d;
+    float sd_f, kh_f, dr_f, pad_f;
 };
 
 // per ensemble, updated on the device by the trajectory kernels
@@ -89,7 +102,7 @@ struct Batch {
     BatchRun *run = nullptr;
     uint2 *chunks = nullptr;    // {ensemble, first site}
     uint64_t *keys = nullptr;   // Philox key of each ensemble
-    double *partial = nullptr;  // 3 rows of n_chunks
+    double *partial = nullptr;  // batch_partial_rows(dim) rows of n_chunks
     unsigned int *done = nullptr; // last-block counter of the per-ensemble kernels
     int *flag = nullptr;          // device: 1 while a projection is unfinished
     int *h_flag = nullptr;        // pinned host mirror
@@ -106,6 +119,7 @@ struct Batch {
     cudaGraphExec_t exec = nullptr;
     cudaStream_t cap_stream = nullptr; // stream used to capture the projection loop body
     cudaStream_t own_stream = nullptr; // the batch's stream unless lq_batch_set_stream names one
+    double coef_dt = -1.0; // dt of the kh / dr coefficients in the ensemble table
     double g_dt = 0.0;
     int g_steps = 0, g_max_gauss = 0, g_flags = 0, g_link_update = -1;
     long long graph_launches = 0;
@@ -133,7 +147,8 @@ struct BatchOps {
     cudaError_t (*gauss)(Batch &b, int ein, int gout);
     cudaError_t (*sweep)(Batch &b, int ein, int eout, int gin, int gout);
     cudaError_t (*check)(Batch &b, int steps_added, int max_steps, cudaGraphConditionalHandle h, int use_handle);
-    cudaError_t (*md)(Batch &b, int rin, int rout, int ein, int eout, int mode, double h1, double h2, double dt);
+    // kick (k1 = kh when k1_on, else 0; k2 = kh) and drift with the coefficients of the table
+    cudaError_t (*md)(Batch &b, int rin, int rout, int ein, int eout, int mode, int k1_on);
     cudaError_t (*plaquette_delta)(Batch &b, int r_old, int r_new);
     cudaError_t (*sumsq_delta)(Batch &b, int e_old, int e_new);
     cudaError_t (*accept)(Batch &b, int r_final);

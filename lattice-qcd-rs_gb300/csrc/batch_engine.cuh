@@ -59,6 +59,12 @@ __device__ __forceinline__ void link_item(uint32_t w, uint32_t n_chunks, int ord
 
 __device__ __forceinline__ uint2 key_of(uint64_t k) { return make_uint2((uint32_t)k, (uint32_t)(k >> 32)); }
 
+// a table coefficient in the arithmetic type
+template <typename T> __device__ __forceinline__ T coef(float f, double d) {
+    if constexpr (sizeof(T) == 4) return f;
+    else return d;
+}
+
 // ------------------------------------------------------------------ trajectory kernels
 // E[eout] <- Normal(0, 0.5 / beta) per ensemble, Philox key keys[e] and counter run[e].counter
 // (k_efield_normal's stream for that seed and counter); also opens the trajectory's
@@ -83,7 +89,7 @@ __global__ void __launch_bounds__(128) k_normal_batch(BView<T> v, int eout, int 
         const unsigned long long ctr = v.run[c.x].counter;
         const size_t eb = (size_t)en.tile0 * (D * 8 * kTile);
         efield_normal_link<D, T, COMP>(sel_e(v, eout) + eb, site, mu, key_of(v.keys[c.x]), (uint32_t)ctr,
-                                       (uint32_t)(ctr >> 32), (T)(0.5 / en.beta), v.elo);
+                                       (uint32_t)(ctr >> 32), coef<T>(en.sd_f, en.sd_d), v.elo);
     }
 }
 
@@ -175,8 +181,7 @@ static __global__ void __launch_bounds__(1024) k_check_batch(const BatchEns *__r
 
 template <int D, typename T, bool COMP, int MODE>
 __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md_batch(BView<T> v, int rin, int rout, int ein,
-                                                                    int eout, double h1, double h2, double dt,
-                                                                    int order) {
+                                                                    int eout, int k1_on, int order) {
     const uint32_t n_work = v.n_chunks * D;
     for (uint32_t w = blockIdx.x; w < n_work; w += gridDim.x) {
         uint32_t chunk;
@@ -188,35 +193,38 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md_batch(BView<T> v, 
         if (site >= en.V) continue;
         const int cur = v.run[c.x].cur;
         const size_t ub = (size_t)en.tile0 * (D * 9 * kTile), eb = (size_t)en.tile0 * (D * 8 * kTile);
-        // the single-lattice coefficients (Engine::md), per ensemble
-        const double ce = -sqrt(2.0 / 3.0) / en.size;
-        const double cu = sqrt(2.0 * 3.0) / en.size * dt;
+        const T kh = coef<T>(en.kh_f, en.kh_d);
         md_link<D, T, COMP, MODE>(sel_u(v, (cur + rin) % 3) + ub, sel_u(v, (cur + rout) % 3) + ub, sel_e(v, ein) + eb,
-                                  sel_e(v, eout) + eb, geo_of<D>(en), site, mu, (T)(h1 * ce), (T)(h2 * ce), (T)cu,
-                                  v.ulo, v.elo);
+                                  sel_e(v, eout) + eb, geo_of<D>(en), site, mu, k1_on ? kh : T(0), kh,
+                                  coef<T>(en.dr_f, en.dr_d), v.ulo, v.elo);
     }
 }
 
-// partial row 0 <- per-chunk sum Re Tr[P(U[r_new]) - P(U[r_old])]
+// partials[chunk * NP + plane] <- sum Re Tr[P(U[r_new]) - P(U[r_old])] of the chunk's plaquettes
+// in one plane (k_plaquette_delta's blocks), NP = D (D - 1) / 2
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_plaquette_delta_batch(BView<T> v, int r_old, int r_new) {
-    for (uint32_t chunk = blockIdx.x; chunk < v.n_chunks; chunk += gridDim.x) {
-        const uint2 c = v.chunks[chunk];
+    constexpr int NP = D * (D - 1) / 2;
+    const uint32_t n_work = v.n_chunks * NP;
+    for (uint32_t w = blockIdx.x; w < n_work; w += gridDim.x) {
+        const uint2 c = v.chunks[w / NP];
         const BatchEns &en = v.ens[c.x];
         const uint32_t site = c.y + threadIdx.x;
+        int mu, nu;
+        plane_dirs<D>((int)(w % NP), mu, nu);
         double r[1] = {0.0};
         if (site < en.V) {
             const int cur = v.run[c.x].cur;
             const size_t ub = (size_t)en.tile0 * (D * 9 * kTile);
-            r[0] = plaquette_delta_site<D, T, COMP>(sel_u(v, (cur + r_old) % 3) + ub, sel_u(v, (cur + r_new) % 3) + ub,
-                                                    geo_of<D>(en), site, v.ulo);
+            r[0] = plaquette_delta_one<D, T, COMP>(sel_u(v, (cur + r_old) % 3) + ub, sel_u(v, (cur + r_new) % 3) + ub,
+                                                   geo_of<D>(en), site, mu, nu, v.ulo);
         }
-        block_reduce_store<1>(r, v.partial, chunk, v.n_chunks);
+        block_reduce_store<1>(r, v.partial, w, n_work);
         __syncthreads();
     }
 }
 
-// partial row 1 <- per-chunk sum (e' - e)(e' + e) of E[e_old] -> E[e_new]
+// partials[NP * n_chunks + chunk] <- per-chunk sum (e' - e)(e' + e) of E[e_old] -> E[e_new]
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_sumsq_delta_batch(BView<T> v, int e_old, int e_new) {
     for (uint32_t chunk = blockIdx.x; chunk < v.n_chunks; chunk += gridDim.x) {
@@ -238,7 +246,7 @@ __global__ void __launch_bounds__(128) k_sumsq_delta_batch(BView<T> v, int e_old
             }
         }
         double r[1] = {(double)acc};
-        block_reduce_store<1>(r, v.partial + v.n_chunks, chunk, v.n_chunks);
+        block_reduce_store<1>(r, v.partial + (size_t)(D * (D - 1) / 2) * v.n_chunks, chunk, v.n_chunks);
         __syncthreads();
     }
 }
@@ -268,14 +276,15 @@ __global__ void __launch_bounds__(128) k_plaquette_batch(BView<T> v, int role) {
 static __global__ void __launch_bounds__(1024) k_accept_batch(const BatchEns *__restrict__ ens, BatchRun *run,
                                                        const uint64_t *__restrict__ keys,
                                                        const double *__restrict__ partial, uint32_t n_chunks,
-                                                       int r_final, BatchResult *results, int result_rows) {
+                                                       int n_planes, int r_final, BatchResult *results,
+                                                       int result_rows) {
     const int e = blockIdx.x;
     const BatchEns en = ens[e];
     double v[2] = {0.0, 0.0};
-    for (uint32_t k = threadIdx.x; k < en.nchunks; k += blockDim.x) {
-        v[0] += partial[en.chunk0 + k];
-        v[1] += partial[n_chunks + en.chunk0 + k];
-    }
+    // the plaquette partials of an ensemble are contiguous (chunk-major, plane-minor)
+    const double *pd = partial + (size_t)en.chunk0 * n_planes;
+    for (uint32_t k = threadIdx.x; k < en.nchunks * (uint32_t)n_planes; k += blockDim.x) v[0] += pd[k];
+    for (uint32_t k = threadIdx.x; k < en.nchunks; k += blockDim.x) v[1] += partial[(size_t)n_planes * n_chunks + en.chunk0 + k];
     __shared__ double res[2];
     block_reduce_store<2>(v, res, 0, 1);
     __syncthreads();
@@ -429,13 +438,13 @@ template <int D, typename T, bool COMP> struct BatchEngine {
                                                       b.flag, h, use_handle);
         return cudaGetLastError();
     }
-    static cudaError_t md(Batch &b, int rin, int rout, int ein, int eout, int mode, double h1, double h2, double dt) {
+    static cudaError_t md(Batch &b, int rin, int rout, int ein, int eout, int mode, int k1_on) {
         const uint32_t n = b.n_chunks * D;
         const uint32_t gsz = grid(b, BK_MD, n);
         const int order = b.shape[BK_MD].order;
         const BView<T> v = view(b);
 #define LQ_MDB_CASE(M)                                                                                                 \
-    case (M): k_md_batch<D, T, COMP, (M)><<<gsz, kChunk, 0, b.stream>>>(v, rin, rout, ein, eout, h1, h2, dt, order); break;
+    case (M): k_md_batch<D, T, COMP, (M)><<<gsz, kChunk, 0, b.stream>>>(v, rin, rout, ein, eout, k1_on, order); break;
         switch (mode) {
             LQ_MDB_CASE(MD_KICK)
             LQ_MDB_CASE(MD_KICK | MD_DRIFT)
@@ -448,7 +457,7 @@ template <int D, typename T, bool COMP> struct BatchEngine {
     }
     static cudaError_t plaquette_delta(Batch &b, int r_old, int r_new) {
         k_plaquette_delta_batch<D, T, COMP>
-            <<<grid(b, BK_PLAQ_DELTA, b.n_chunks), kChunk, 0, b.stream>>>(view(b), r_old, r_new);
+            <<<grid(b, BK_PLAQ_DELTA, b.n_chunks * (D * (D - 1) / 2)), kChunk, 0, b.stream>>>(view(b), r_old, r_new);
         return cudaGetLastError();
     }
     static cudaError_t sumsq_delta(Batch &b, int e_old, int e_new) {
@@ -457,8 +466,8 @@ template <int D, typename T, bool COMP> struct BatchEngine {
         return cudaGetLastError();
     }
     static cudaError_t accept(Batch &b, int r_final) {
-        k_accept_batch<<<b.n_ens, 1024, 0, b.stream>>>(b.ens, b.run, b.keys, b.partial, b.n_chunks, r_final, b.results,
-                                                       b.result_rows);
+        k_accept_batch<<<b.n_ens, 1024, 0, b.stream>>>(b.ens, b.run, b.keys, b.partial, b.n_chunks, D * (D - 1) / 2,
+                                                       r_final, b.results, b.result_rows);
         return cudaGetLastError();
     }
     static cudaError_t plaquette(Batch &b, int role) {

@@ -57,9 +57,13 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
     // out <- scale * Im Tr(T^a U_mu(x) Sigma_mu(x)) on every link (out zeroed by the caller)
+    // launch shape of k_md: 128 sites of one direction per block, directions fastest (a shape of
+    // 32 sites x D directions per block measured 13% slower at 32^4)
+    static dim3 md_grid_k(const State &s) { return dim3(((s.V + 127) / 128) * D, 1, 1); }
+    static unsigned md_block_k() { return 128; }
     static cudaError_t force(State &s, const void *U, void *out, double scale) {
-        const dim3 grid(((s.V + 127) / 128) * D, 1, 1);
-        k_md<D, T, COMP, MD_KICK><<<grid, 128, 0, s.stream>>>((const V2<T> *)U, (V2<T> *)U, (const T *)out, (T *)out,
+        const dim3 grid = md_grid_k(s);
+        k_md<D, T, COMP, MD_KICK><<<grid, md_block_k(), 0, s.stream>>>((const V2<T> *)U, (V2<T> *)U, (const T *)out, (T *)out,
                                                                geo(s), T(0), (T)scale, T(0));
         return cudaGetLastError();
     }
@@ -81,13 +85,14 @@ template <int D, typename T, bool COMP> struct Engine {
         const double cu = sqrt(2.0 * 3.0) / s.size * dt;
         const T k1 = (T)(h1 * ce), k2 = (T)(h2 * ce), drift = (T)cu;
         const Geo<D> g = geo(s);
-        const dim3 grid(((s.V + 127) / 128) * D, 1, 1); // mu fastest, see k_md
+        const dim3 grid = md_grid_k(s);
+        const unsigned block = md_block_k();
         const V2<T> *in = (const V2<T> *)Uin;
         V2<T> *out = (V2<T> *)Uout;
         const T *ei = (const T *)Ein;
         T *eo = (T *)Eout;
 #define LQ_MD_CASE(M)                                                                                                  \
-    case (M): k_md<D, T, COMP, (M)><<<grid, 128, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
+    case (M): k_md<D, T, COMP, (M)><<<grid, block, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
         switch (mode) {
             LQ_MD_CASE(MD_KICK)
             LQ_MD_CASE(MD_DRIFT)
@@ -136,7 +141,7 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
     static cudaError_t plaquette_delta(State &s, const void *Uold, const void *Unew, uint32_t *n_partials) {
-        const uint32_t blocks = (s.V + 127) / 128;
+        const uint32_t blocks = (s.V + 127) / 128 * (D * (D - 1) / 2); // one block per 128 sites and plane
         k_plaquette_delta<D, T, COMP>
             <<<blocks, 128, 0, s.stream>>>((const V2<T> *)Uold, (const V2<T> *)Unew, geo(s), s.partial);
         *n_partials = blocks;

@@ -49,6 +49,7 @@ template <typename T> using V2 = typename vec2_t<T>::type;
 #ifndef LQ_SWEEP_MIN_BLOCKS
 #define LQ_SWEEP_MIN_BLOCKS 5
 #endif
+
 template <typename T> struct MinBlocks {
     static constexpr int md = sizeof(T) == 4 ? LQ_MD_MIN_BLOCKS : 1;
     static constexpr int sweep = sizeof(T) == 4 ? LQ_SWEEP_MIN_BLOCKS : 1;
@@ -356,7 +357,7 @@ __device__ __forceinline__ double gauss_site(const V2<T> *__restrict__ U, const 
             load_mat<T>(U + tix(xm, D * 9, mu * 9), u);
             adjoint_to_matrix<T>(ex_c, ex_m);
             adj_mul<T>(em_c, u, t);
-            mul_an(u, t, w);
+            mul_an_herm(u, t, w); // U^dag E U is Hermitian
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
                 gs.e[k].re += ex_m.e[k].re - w.e[k].re;
@@ -389,12 +390,11 @@ __global__ void __launch_bounds__(256) k_gauss(const V2<T> *__restrict__ U, cons
 template <typename T, bool COMP>
 __device__ __forceinline__ void projection_step(const mat3<T> &u, const mat3<T> &gx, const T *gxc, const mat3<T> &gp,
                                                 T *e, T *el) {
-    mat3<T> t1, t2, x;
+    mat3<T> t1, t2;
     mul_nn(u, gx, t1);
-    mul_na(t1, u, t2);
-    mul_nn(t2, gp, x);
+    mul_na_herm(t1, u, t2); // u G(x) u^dag is Hermitian
     T xc[8];
-    two_re_tr_generators(x, xc);
+    two_re_tr_generators_of_product(t2, gp, xc);
     const T K = T(0.12);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -495,7 +495,7 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
                 }
                 projection_step<T, COMP>(w, gm, gmc, gx, e, el);
                 adj_mul<T>(e, w, t);
-                mul_an(w, t, wm);
+                mul_an_herm(w, t, wm); // U^dag E' U is Hermitian
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
                     gnew.e[k].re -= wm.e[k].re;
@@ -583,97 +583,110 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
 // needs only products with one difference factor, so FP32 products leave an error
 // proportional to |dU|, not to |U|.  dU = (hi' - hi) + (lo' - lo) keeps the compensated part.
 // Partial: sum Re Tr(P' - P) (Delta hamiltonian_links = -beta/3 times it).
+// planes (mu, nu), mu < nu, in the order (0,1), (0,2), ..., (D-2, D-1)
+template <int D> __device__ __forceinline__ void plane_dirs(int p, int &mu, int &nu) {
+    mu = 0;
+#pragma unroll
+    for (int m = 0; m < D - 1; ++m) {
+        const int n_in_row = D - 1 - m;
+        if (p >= n_in_row) {
+            p -= n_in_row;
+            mu = m + 1;
+        } else {
+            break;
+        }
+    }
+    nu = mu + 1 + p;
+}
+
+// Re Tr[P(U') - P(U)] of the plaquette (x; mu, nu) of one thread (see k_plaquette_delta)
 template <int D, typename T, bool COMP>
-__device__ __forceinline__ double plaquette_delta_site(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
-                                                       const Geo<D> &g, uint32_t site, size_t ulo) {
-    {
-        uint32_t c[D];
-        site_coords(g, site, c);
-        auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
-            const size_t i = tix(x, D * 9, dir * 9);
-            load_mat<T>(Uo + i, old_hi);
-            load_mat<T>(Un + i, new_hi);
-            if (COMP) {
-                mat3<T> ol, nl;
-                load_mat<T>(Uo + ulo + i, ol);
-                load_mat<T>(Un + ulo + i, nl);
-#pragma unroll
-                for (int k = 0; k < 9; ++k) {
-                    diff.e[k].re = (new_hi.e[k].re - old_hi.e[k].re) + (nl.e[k].re - ol.e[k].re);
-                    diff.e[k].im = (new_hi.e[k].im - old_hi.e[k].im) + (nl.e[k].im - ol.e[k].im);
-                }
-            } else {
-#pragma unroll
-                for (int k = 0; k < 9; ++k) {
-                    diff.e[k].re = new_hi.e[k].re - old_hi.e[k].re;
-                    diff.e[k].im = new_hi.e[k].im - old_hi.e[k].im;
-                }
-            }
-        };
-        // Re Tr(X Y) and Re Tr(X Y^dag)
-        auto re_tr_nn = [](const mat3<T> &x, const mat3<T> &y) {
-            T s = T(0);
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    s = fma(x.e[i * 3 + k].re, y.e[k * 3 + i].re, s);
-                    s = fma(-x.e[i * 3 + k].im, y.e[k * 3 + i].im, s);
-                }
-            return s;
-        };
-        auto re_tr_na = [](const mat3<T> &x, const mat3<T> &y) {
-            T s = T(0);
+__device__ __forceinline__ double plaquette_delta_one(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
+                                                      const Geo<D> &g, uint32_t site, int mu, int nu, size_t ulo) {
+    uint32_t c[D];
+    site_coords(g, site, c);
+    auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
+        const size_t i = tix(x, D * 9, dir * 9);
+        load_mat<T>(Uo + i, old_hi);
+        load_mat<T>(Un + i, new_hi);
+        if (COMP) {
+            mat3<T> ol, nl;
+            load_mat<T>(Uo + ulo + i, ol);
+            load_mat<T>(Un + ulo + i, nl);
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                s = fma(x.e[k].re, y.e[k].re, s);
-                s = fma(x.e[k].im, y.e[k].im, s);
+                diff.e[k].re = (new_hi.e[k].re - old_hi.e[k].re) + (nl.e[k].re - ol.e[k].re);
+                diff.e[k].im = (new_hi.e[k].im - old_hi.e[k].im) + (nl.e[k].im - ol.e[k].im);
             }
-            return s;
-        };
-        T acc = T(0);
-#pragma unroll 1
-        for (int mu = 0; mu < D; ++mu) {
-            const uint32_t xpmu = fwd(g, site, c[mu], mu);
-#pragma unroll 1
-            for (int nu = mu + 1; nu < D; ++nu) {
-                const uint32_t xpnu = fwd(g, site, c[nu], nu);
-                // links: A = U_mu(x), B = U_nu(x+mu), C = U_mu(x+nu), Dd = U_nu(x); primes: new.
-                // Evaluated in an order that keeps about four matrices live.
-                mat3<T> q1, t, s1, x_old, x_new, dx, l1;
-                T term = T(0);
-                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
-                load_mat<T>(Un + tix(xpnu, D * 9, mu * 9), t);     // C'
-                mul_nn(x_new, t, q1);                                  // Q1 = Dd' C'
-                load_mat<T>(Un + tix(xpmu, D * 9, nu * 9), t);     // B'
-                mul_na(t, q1, s1);                                     // B' C'^dag Dd'^dag
-                load_pair(mu, site, x_old, x_new, dx);                 // A, A', dA
-                term += re_tr_nn(dx, s1);                              // Tr(dA B' C'^dag Dd'^dag)
-                mul_an(q1, x_old, t);                                  // C'^dag Dd'^dag A
-                mat3<T> a_old = x_old;
-                load_pair(nu, xpmu, x_old, x_new, dx);                 // B, B', dB
-                term += re_tr_nn(dx, t);                               // Tr(A dB C'^dag Dd'^dag)
-                mul_nn(a_old, x_old, l1);                              // L1 = A B
-                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
-                mul_an(x_new, l1, t);                                  // Dd'^dag A B
-                load_pair(mu, xpnu, x_old, x_new, dx);                 // C, C', dC
-                term += re_tr_na(t, dx);                               // Tr(A B dC^dag Dd'^dag)
-                mul_na(l1, x_old, t);                                  // A B C^dag
-                load_pair(nu, site, x_old, x_new, dx);                 // Dd, Dd', dDd
-                term += re_tr_na(t, dx);                               // Tr(A B C^dag dDd^dag)
-                acc += term;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                diff.e[k].re = new_hi.e[k].re - old_hi.e[k].re;
+                diff.e[k].im = new_hi.e[k].im - old_hi.e[k].im;
             }
         }
-        return (double)acc;
-    }
+    };
+    // Re Tr(X Y) and Re Tr(X Y^dag)
+    auto re_tr_nn = [](const mat3<T> &x, const mat3<T> &y) {
+        T s = T(0);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                s = fma(x.e[i * 3 + k].re, y.e[k * 3 + i].re, s);
+                s = fma(-x.e[i * 3 + k].im, y.e[k * 3 + i].im, s);
+            }
+        return s;
+    };
+    auto re_tr_na = [](const mat3<T> &x, const mat3<T> &y) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            s = fma(x.e[k].re, y.e[k].re, s);
+            s = fma(x.e[k].im, y.e[k].im, s);
+        }
+        return s;
+    };
+    const uint32_t xpmu = fwd(g, site, c[mu], mu);
+    const uint32_t xpnu = fwd(g, site, c[nu], nu);
+    // links: A = U_mu(x), B = U_nu(x+mu), C = U_mu(x+nu), Dd = U_nu(x); primes: new.
+    // Evaluated in an order that keeps about four matrices live.
+    mat3<T> q1, t, s1, x_old, x_new, dx, l1;
+    T term = T(0);
+    load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
+    load_mat<T>(Un + tix(xpnu, D * 9, mu * 9), t);     // C'
+    mul_nn(x_new, t, q1);                                  // Q1 = Dd' C'
+    load_mat<T>(Un + tix(xpmu, D * 9, nu * 9), t);     // B'
+    mul_na(t, q1, s1);                                     // B' C'^dag Dd'^dag
+    load_pair(mu, site, x_old, x_new, dx);                 // A, A', dA
+    term += re_tr_nn(dx, s1);                              // Tr(dA B' C'^dag Dd'^dag)
+    mul_an(q1, x_old, t);                                  // C'^dag Dd'^dag A
+    mat3<T> a_old = x_old;
+    load_pair(nu, xpmu, x_old, x_new, dx);                 // B, B', dB
+    term += re_tr_nn(dx, t);                               // Tr(A dB C'^dag Dd'^dag)
+    mul_nn(a_old, x_old, l1);                              // L1 = A B
+    load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
+    mul_an(x_new, l1, t);                                  // Dd'^dag A B
+    load_pair(mu, xpnu, x_old, x_new, dx);                 // C, C', dC
+    term += re_tr_na(t, dx);                               // Tr(A B dC^dag Dd'^dag)
+    mul_na(l1, x_old, t);                                  // A B C^dag
+    load_pair(nu, site, x_old, x_new, dx);                 // Dd, Dd', dDd
+    term += re_tr_na(t, dx);                               // Tr(A B C^dag dDd^dag)
+    return (double)term;
 }
+// One thread per plaquette: block b covers sites (b / NP) * 128 .. +127 of plane b % NP (planes
+// fastest, so the planes of a block of sites run together and share their links in L2);
+// partial b.  NP = D (D - 1) / 2.
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
                                                          Geo<D> g, double *__restrict__ partial) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr int NP = D * (D - 1) / 2;
+    const uint32_t site = (blockIdx.x / NP) * blockDim.x + threadIdx.x;
+    int mu, nu;
+    plane_dirs<D>((int)(blockIdx.x % NP), mu, nu);
     double v[1] = {0.0};
     if (site < g.V)
-        v[0] = plaquette_delta_site<D, T, COMP>(Uo, Un, g, site, (size_t)tiles_of(g.V) * D * 9 * kTile);
+        v[0] = plaquette_delta_one<D, T, COMP>(Uo, Un, g, site, mu, nu, (size_t)tiles_of(g.V) * D * 9 * kTile);
     block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
 }
 

@@ -319,7 +319,7 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
     alloc(&s->E_alt, s->efield_bytes(), __LINE__);
     alloc(&s->G, s->gauss_bytes(), __LINE__);
     alloc(&s->G_alt, s->gauss_bytes(), __LINE__);
-    alloc((void **)&s->partial, sizeof(double) * 3 * (size_t)s->partial_slots, __LINE__);
+    alloc((void **)&s->partial, sizeof(double) * lq::kPartialRows * (size_t)s->partial_slots, __LINE__);
     alloc((void **)&s->d_out, sizeof(double) * 16, __LINE__);
     if (!rc) {
         cudaError_t e = cudaMallocHost((void **)&s->h_out, sizeof(double) * 16);
@@ -416,7 +416,7 @@ int lq_state_device_bytes(const lq_state *s, size_t *bytes) {
     LQ_CHECK_STATE(s);
     if (!bytes) return LQ_ERR_INVALID_ARGUMENT;
     *bytes = 3 * s->link_bytes() + 2 * s->efield_bytes() + 2 * s->gauss_bytes() +
-             sizeof(double) * (3 * (size_t)s->partial_slots + 16) + s->staging_bytes;
+             sizeof(double) * (lq::kPartialRows * (size_t)s->partial_slots + 16) + s->staging_bytes;
     return LQ_OK;
 }
 

@@ -125,6 +125,23 @@ int ensure_results(Batch &b, int rows) {
     return LQ_OK;
 }
 
+// the kick and drift coefficients of every ensemble for step dt, in the single-lattice path's
+// arithmetic (Engine::md): kh = (dt/2) (-sqrt(2/3) / size), dr = sqrt(6) / size * dt
+int set_step_coefficients(Batch &b, double dt) {
+    if (b.coef_dt == dt) return LQ_OK;
+    for (auto &en : b.ens_h) {
+        const double ce = -std::sqrt(2.0 / 3.0) / en.size;
+        en.kh_d = (dt / 2.0) * ce;
+        en.dr_d = std::sqrt(2.0 * 3.0) / en.size * dt;
+        en.kh_f = (float)en.kh_d;
+        en.dr_f = (float)en.dr_d;
+    }
+    BK(cudaStreamSynchronize(b.stream));
+    BK(cudaMemcpy(b.ens, b.ens_h.data(), sizeof(lq::BatchEns) * b.ens_h.size(), cudaMemcpyHostToDevice));
+    b.coef_dt = dt;
+    return LQ_OK;
+}
+
 // state buffer index of ensemble e (run[e].cur), read back from the device
 int state_buffer(Batch &b, int e, int *buf) {
     lq::BatchRun r;
@@ -160,16 +177,18 @@ int enqueue_md_accept(Batch &b, double dt, int n, int flags) {
         const size_t half = b.efield_bytes() / 2;
         BK(cudaMemsetAsync((char *)b.E[1] + half, 0, half, b.stream));
     }
+    // the coefficients of dt are in the ensemble table (set_step_coefficients)
+    (void)dt;
     const int KD = lq::MD_KICK | lq::MD_DRIFT | link_update_bits(b.link_update);
-    BK(b.ops->md(b, 0, 1, 1, 0, KD, 0.0, dt / 2.0, dt));
+    BK(b.ops->md(b, 0, 1, 1, 0, KD, 0));
     int cur = 1, nxt = 2;
     for (int i = 1; i < n; ++i) {
-        BK(b.ops->md(b, cur, nxt, 0, 0, KD, dt / 2.0, dt / 2.0, dt));
+        BK(b.ops->md(b, cur, nxt, 0, 0, KD, 1));
         const int t = cur;
         cur = nxt;
         nxt = t;
     }
-    BK(b.ops->md(b, cur, cur, 0, 0, lq::MD_KICK, 0.0, dt / 2.0, 0.0));
+    BK(b.ops->md(b, cur, cur, 0, 0, lq::MD_KICK, 0));
     BK(b.ops->plaquette_delta(b, 0, cur));
     BK(b.ops->sumsq_delta(b, 1, 0));
     BK(b.ops->accept(b, cur));
@@ -262,9 +281,7 @@ int time_class(Batch &b, int cls, double dt, int reps, float *ms) {
     int rc = LQ_OK;
     auto launch = [&]() -> cudaError_t {
         switch (cls) {
-        case lq::BK_MD:
-            return b.ops->md(b, 0, 1, 1, 0, lq::MD_KICK | lq::MD_DRIFT | link_update_bits(b.link_update), dt / 2.0,
-                             dt / 2.0, dt);
+        case lq::BK_MD: return b.ops->md(b, 0, 1, 1, 0, lq::MD_KICK | lq::MD_DRIFT | link_update_bits(b.link_update), 1);
         case lq::BK_SWEEP: return b.ops->sweep(b, 0, 1, 0, 1);
         case lq::BK_GAUSS: return b.ops->gauss(b, 0, 0);
         case lq::BK_PLAQ_DELTA: return b.ops->plaquette_delta(b, 0, 1);
@@ -353,6 +370,8 @@ int lq_batch_create(int dim, int n_ensembles, const int *L, const double *size, 
         en.nchunks = (uint32_t)((V + lq::kChunk - 1) / lq::kChunk);
         en.size = size[e];
         en.beta = beta[e];
+        en.sd_d = 0.5 / beta[e]; // Engine::efield_normal's standard deviation
+        en.sd_f = (float)en.sd_d;
         tiles += (V + 31) / 32;
         chunks += en.nchunks;
         links += V * (uint64_t)dim;
@@ -387,7 +406,7 @@ int lq_batch_create(int dim, int n_ensembles, const int *L, const double *size, 
     alloc((void **)&b->run, sizeof(lq::BatchRun) * n_ensembles, __LINE__);
     alloc((void **)&b->chunks, sizeof(uint2) * chunks, __LINE__);
     alloc((void **)&b->keys, sizeof(uint64_t) * n_ensembles, __LINE__);
-    alloc((void **)&b->partial, sizeof(double) * 3 * chunks, __LINE__);
+    alloc((void **)&b->partial, sizeof(double) * lq::batch_partial_rows(dim) * chunks, __LINE__);
     alloc((void **)&b->done, sizeof(unsigned int), __LINE__);
     alloc((void **)&b->flag, sizeof(int), __LINE__);
     if (!rc) {
@@ -405,7 +424,8 @@ int lq_batch_create(int dim, int n_ensembles, const int *L, const double *size, 
             e = cudaMemsetAsync(b->E[i], 0, b->efield_bytes(), b->stream);
             if (e == cudaSuccess) e = cudaMemsetAsync(b->G[i], 0, b->gauss_bytes(), b->stream);
         }
-        if (e == cudaSuccess) e = cudaMemsetAsync(b->partial, 0, sizeof(double) * 3 * chunks, b->stream);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(b->partial, 0, sizeof(double) * lq::batch_partial_rows(dim) * chunks, b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(b->done, 0, sizeof(unsigned int), b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(b->flag, 0, sizeof(int), b->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
@@ -457,7 +477,8 @@ int lq_batch_info(const lq_batch *b, int *dim, int *n_ensembles, long long *tota
     if (total_links) *total_links = (long long)b->total_links;
     if (device_bytes)
         *device_bytes = 3 * b->link_bytes() + 2 * b->efield_bytes() + 2 * b->gauss_bytes() +
-                        sizeof(double) * 3 * (size_t)b->n_chunks + sizeof(uint2) * (size_t)b->n_chunks +
+                        sizeof(double) * lq::batch_partial_rows(b->dim) * (size_t)b->n_chunks +
+                        sizeof(uint2) * (size_t)b->n_chunks +
                         (sizeof(lq::BatchEns) + sizeof(lq::BatchRun) + 8) * (size_t)b->n_ens;
     return LQ_OK;
 }
@@ -561,13 +582,18 @@ int lq_batch_autotune(lq_batch *b, double dt, int reps) {
     BK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     BK(cudaStreamSynchronize(b->stream));
     drop_graph(*b);
+    int rc0 = set_step_coefficients(*b, dt);
+    if (rc0) return rc0;
     // inputs for the timed launches: a fresh draw and its Gauss law (E is scratch between
     // trajectories; the state's links are only read)
     BK(b->ops->normal(*b, 0));
     BK(b->ops->gauss(*b, 0, 0));
     for (int cls = 0; cls < lq::BK_CLASSES; ++cls) {
         const bool per_link = cls == lq::BK_MD || cls == lq::BK_NORMAL;
-        const uint32_t n_work = b->n_chunks * (per_link ? (uint32_t)b->dim : 1u);
+        const uint32_t per_chunk = per_link ? (uint32_t)b->dim
+                                   : cls == lq::BK_PLAQ_DELTA ? (uint32_t)(b->dim * (b->dim - 1) / 2)
+                                                                : 1u;
+        const uint32_t n_work = b->n_chunks * per_chunk;
         const int occ = b->ops->occupancy(cls);
         std::vector<uint32_t> grids = {0};
         if (occ > 0)
@@ -612,6 +638,7 @@ int lq_batch_hmc_run(lq_batch *b, double dt, int n_steps, int n_trajectories, in
         return LQ_ERR_INVALID_ARGUMENT;
     const int max_steps = max_gauss_steps > 0 ? max_gauss_steps : kDefaultMaxGaussSteps;
     int rc = ensure_results(*b, n_trajectories);
+    if (!rc) rc = set_step_coefficients(*b, dt);
     if (rc) return rc;
     lq::k_batch_setup<<<1, 256, 0, b->stream>>>(b->keys, b->run, b->n_ens, 0, 0, 2);
     BK(cudaGetLastError());

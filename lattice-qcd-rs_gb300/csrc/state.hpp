@@ -122,8 +122,10 @@ const Ops *ops_f64(int dim);
 const Ops *ops_f32(int dim);
 const Ops *ops_mixed(int dim);
 
-// partial slots needed for V sites
+// partial slots needed for V sites (per row), and the rows of the partial buffer: the plaquette
+// difference keeps one partial per 128 sites and plane, D (D - 1) / 2 <= 6 planes
 inline uint32_t partial_slots_for(uint32_t V) { return (V + 127) / 128 + 64; }
+constexpr int kPartialRows = 6;
 
 } // namespace lq
 

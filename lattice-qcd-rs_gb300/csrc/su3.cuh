@@ -105,6 +105,70 @@ template <typename T> __device__ __forceinline__ void mul_an(const mat3<T> &a, c
         }
 }
 
+// r = a * b^dagger for a product known to be Hermitian (u G u^dag with G Hermitian): the upper
+// triangle is computed as mul_na computes it, the diagonal's real part likewise (its imaginary part
+// is zero), and the lower triangle is the conjugate of the upper one -- 54 multiply-adds, not 108.
+template <typename T> __device__ __forceinline__ void mul_na_herm(const mat3<T> &a, const mat3<T> &b, mat3<T> &r) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        T d = a.e[i * 3].re * b.e[i * 3].re;
+        d = fma(a.e[i * 3].im, b.e[i * 3].im, d);
+#pragma unroll
+        for (int k = 1; k < 3; ++k) {
+            d = fma(a.e[i * 3 + k].re, b.e[i * 3 + k].re, d);
+            d = fma(a.e[i * 3 + k].im, b.e[i * 3 + k].im, d);
+        }
+        r.e[i * 4] = cmk(d, T(0));
+#pragma unroll
+        for (int j = i + 1; j < 3; ++j) {
+            T re = a.e[i * 3].re * b.e[j * 3].re;
+            T im = -a.e[i * 3].re * b.e[j * 3].im;
+            re = fma(a.e[i * 3].im, b.e[j * 3].im, re);
+            im = fma(a.e[i * 3].im, b.e[j * 3].re, im);
+#pragma unroll
+            for (int k = 1; k < 3; ++k) {
+                re = fma(a.e[i * 3 + k].re, b.e[j * 3 + k].re, re);
+                re = fma(a.e[i * 3 + k].im, b.e[j * 3 + k].im, re);
+                im = fma(-a.e[i * 3 + k].re, b.e[j * 3 + k].im, im);
+                im = fma(a.e[i * 3 + k].im, b.e[j * 3 + k].re, im);
+            }
+            r.e[i * 3 + j] = cmk(re, im);
+            r.e[j * 3 + i] = cmk(re, -im);
+        }
+    }
+}
+
+// r = a^dagger * b for a product known to be Hermitian (U^dag E U): as mul_na_herm
+template <typename T> __device__ __forceinline__ void mul_an_herm(const mat3<T> &a, const mat3<T> &b, mat3<T> &r) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        T d = a.e[i].re * b.e[i].re;
+        d = fma(a.e[i].im, b.e[i].im, d);
+#pragma unroll
+        for (int k = 1; k < 3; ++k) {
+            d = fma(a.e[k * 3 + i].re, b.e[k * 3 + i].re, d);
+            d = fma(a.e[k * 3 + i].im, b.e[k * 3 + i].im, d);
+        }
+        r.e[i * 4] = cmk(d, T(0));
+#pragma unroll
+        for (int j = i + 1; j < 3; ++j) {
+            T re = a.e[i].re * b.e[j].re;
+            T im = a.e[i].re * b.e[j].im;
+            re = fma(a.e[i].im, b.e[j].im, re);
+            im = fma(-a.e[i].im, b.e[j].re, im);
+#pragma unroll
+            for (int k = 1; k < 3; ++k) {
+                re = fma(a.e[k * 3 + i].re, b.e[k * 3 + j].re, re);
+                re = fma(a.e[k * 3 + i].im, b.e[k * 3 + j].im, re);
+                im = fma(a.e[k * 3 + i].re, b.e[k * 3 + j].im, im);
+                im = fma(-a.e[k * 3 + i].im, b.e[k * 3 + j].re, im);
+            }
+            r.e[i * 3 + j] = cmk(re, im);
+            r.e[j * 3 + i] = cmk(re, -im);
+        }
+    }
+}
+
 // r += a * b^dagger
 template <typename T> __device__ __forceinline__ void mul_na_acc(const mat3<T> &a, const mat3<T> &b, mat3<T> &r) {
 #pragma unroll
@@ -181,6 +245,46 @@ template <typename T> __device__ __forceinline__ void im_tr_generators(const mat
     out[5] = h * (x.e[7].im + x.e[5].im);
     out[6] = h * (x.e[5].re - x.e[7].re);
     out[7] = T(kOneOver2Sqrt3) * (x.e[0].im + x.e[4].im) + T(kMinusOneOverSqrt3) * x.e[8].im;
+}
+
+// out^a = 2 Re Tr(T^a a b) without forming the full product: the real parts of the diagonal and
+// the six off-diagonal entries of a b, in mul_nn's order (90 multiply-adds instead of 108)
+template <typename T>
+__device__ __forceinline__ void two_re_tr_generators_of_product(const mat3<T> &a, const mat3<T> &b, T *out) {
+    auto entry = [&](int i, int j) {
+        T re = a.e[i * 3].re * b.e[j].re, im = a.e[i * 3].re * b.e[j].im;
+        re = fma(-a.e[i * 3].im, b.e[j].im, re);
+        im = fma(a.e[i * 3].im, b.e[j].re, im);
+#pragma unroll
+        for (int k = 1; k < 3; ++k) {
+            re = fma(a.e[i * 3 + k].re, b.e[k * 3 + j].re, re);
+            re = fma(-a.e[i * 3 + k].im, b.e[k * 3 + j].im, re);
+            im = fma(a.e[i * 3 + k].re, b.e[k * 3 + j].im, im);
+            im = fma(a.e[i * 3 + k].im, b.e[k * 3 + j].re, im);
+        }
+        return cmk(re, im);
+    };
+    auto diag_re = [&](int i) {
+        T re = a.e[i * 3].re * b.e[i].re;
+        re = fma(-a.e[i * 3].im, b.e[i].im, re);
+#pragma unroll
+        for (int k = 1; k < 3; ++k) {
+            re = fma(a.e[i * 3 + k].re, b.e[k * 3 + i].re, re);
+            re = fma(-a.e[i * 3 + k].im, b.e[k * 3 + i].im, re);
+        }
+        return re;
+    };
+    const cpx<T> x1 = entry(0, 1), x3 = entry(1, 0), x2 = entry(0, 2), x6 = entry(2, 0), x5 = entry(1, 2),
+                 x7 = entry(2, 1);
+    const T x0 = diag_re(0), x4 = diag_re(1), x8 = diag_re(2);
+    out[0] = x3.re + x1.re;
+    out[1] = x3.im - x1.im;
+    out[2] = x0 - x4;
+    out[3] = x6.re + x2.re;
+    out[4] = x6.im - x2.im;
+    out[5] = x7.re + x5.re;
+    out[6] = x7.im - x5.im;
+    out[7] = T(2.0 * kOneOver2Sqrt3) * (x0 + x4) + T(2.0 * kMinusOneOverSqrt3) * x8;
 }
 
 // 1/n! evaluated at compile time

@@ -197,7 +197,7 @@ def batch_study(args):
     another as single states (two trajectories each, scaled)."""
     import torch
 
-    n_ens, dt, nmd, size = 64, 0.01, 10, 1000.0
+    n_ens, dt, nmd, size = args.ensembles, 0.01, 10, 1000.0
     Ls = np.random.default_rng(3).choice([8, 10, 12, 16, 20], size=n_ens)
     betas = np.linspace(0.5, 3.5, n_ens)
     peak = hbm_peak()
@@ -210,12 +210,13 @@ def batch_study(args):
     tune_s = time.time() - t0
     stream = torch.cuda.Stream()
     b.set_stream(stream.cuda_stream)
-    b.hmc_run(dt, nmd, 2)  # capture + warm-up
+    graph = not args.eager
+    b.hmc_run(dt, nmd, 2, graph=graph)  # capture + warm-up
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     w0 = time.time()
     e0.record(stream)
-    b.hmc_run(dt, nmd, args.traj, measure_plaquette=True)
+    b.hmc_run(dt, nmd, args.traj, measure_plaquette=True, graph=graph)
     e1.record(stream)
     torch.cuda.synchronize()
     wall = time.time() - w0
@@ -239,6 +240,9 @@ def batch_study(args):
            "max_abs_delta_h": float(np.abs(r["delta_h"][ok]).max()) if ok.any() else None,
            "gauss_steps_range": [int(r["gauss_steps"][ok].min()), int(r["gauss_steps"][ok].max())] if ok.any() else None}
     b.close()
+    if args.quick:
+        print(json.dumps(out), flush=True)
+        return out
     # the same ensembles one after another (the reference's way of scanning), 2 trajectories each
     seq_ms, seq_links = 0.0, 0
     for e in range(n_ens):
@@ -319,6 +323,11 @@ def main():
     ap.add_argument("--traj", type=int, default=None)
     ap.add_argument("--L", type=int, default=32)
     ap.add_argument("--betas", type=float, nargs="*", default=[0.5, 1.0, 2.0, 4.0])
+    ap.add_argument("--quick", action="store_true", help="batch: skip the one-after-another comparison")
+    ap.add_argument("--ensembles", type=int, default=64, help="batch: number of ensembles (the first n draws)")
+    ap.add_argument("--eager", action="store_true",
+                    help="batch: launch the kernels one by one instead of the captured graph (for profilers, "
+                         "which do not see kernels of graphs with conditional nodes)")
     args = ap.parse_args()
     if args.study == "precision":
         args.traj = args.traj or 100

@@ -31,7 +31,7 @@ def _rank(rank, world, port, out):
 
 def test_replica_value_over_two_gloo_ranks():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
         vals = dict(out)

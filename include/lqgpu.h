@@ -172,6 +172,17 @@ int lq_integrate(lq_state *s, int mode, double dt, int n);
 /* simulate_using_leapfrog_n (src/simulation/state.rs:318-357) */
 int lq_leapfrog_n(lq_state *s, double dt, int n);
 
+/* ---------------------------------------------------------------- clover observables
+ * LinkMatrix::f_mu_nu and magnetic_field_vec (src/field.rs:822-871) at every site, from the clover
+ * C_ij = P_ij + P_{j,-i} + P_{-i,-j} + P_{-j,i} (src/field.rs:806-820):
+ *   lq_field_strength: F_ij = (C_ij - C_ji) / (8 size^2) for the planes i < j in the order
+ *     (0,1), (0,2), ..., (D-2,D-1); out double[V][D(D-1)/2][18] (3x3 complex, serde layout);
+ *     F_ji = -F_ij.
+ *   lq_magnetic_field: B_k = sum_{i,j} eps(k,i,j) F_ij / (2i) for k = 0..D-1 with the three-index
+ *     levi_civita (src/utils.rs:306-318); out double[V][D][18] (zero for D = 2). */
+int lq_field_strength(lq_state *s, double *out, size_t n_doubles);
+int lq_magnetic_field(lq_state *s, double *out, size_t n_doubles);
+
 /* ---------------------------------------------------------------- differentiation
  * The gauge force is the adjoint of the Wilson action: a forward / backward pair in the shape of
  * an autograd function.  No reference counterpart as an API; the reference's force is

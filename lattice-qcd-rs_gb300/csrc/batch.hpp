@@ -23,13 +23,6 @@ namespace lq {
 
 constexpr uint32_t kChunk = 128; // sites per chunk = threads per block of the batched kernels
 
-// rows of n_chunks partials: the plaquette difference keeps D (D - 1) / 2 (one per plane), the
-// E-field difference one more; the sweep residuals and plaquette sums use up to three
-inline size_t batch_partial_rows(int dim) {
-    const int np = dim * (dim - 1) / 2;
-    return (size_t)(np + 1 > 3 ? np + 1 : 3);
-}
-
 // per ensemble, constant after creation (device copy)
 struct BatchEns {
     uint32_t V, L, tile0, chunk0, nchunks, pad;
@@ -102,7 +95,7 @@ struct Batch {
     BatchRun *run = nullptr;
     uint2 *chunks = nullptr;    // {ensemble, first site}
     uint64_t *keys = nullptr;   // Philox key of each ensemble
-    double *partial = nullptr;  // batch_partial_rows(dim) rows of n_chunks
+    double *partial = nullptr;  // 3 rows of n_chunks
     unsigned int *done = nullptr; // last-block counter of the per-ensemble kernels
     int *flag = nullptr;          // device: 1 while a projection is unfinished
     int *h_flag = nullptr;        // pinned host mirror

@@ -200,31 +200,26 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md_batch(BView<T> v, 
     }
 }
 
-// partials[chunk * NP + plane] <- sum Re Tr[P(U[r_new]) - P(U[r_old])] of the chunk's plaquettes
-// in one plane (k_plaquette_delta's blocks), NP = D (D - 1) / 2
+// partial row 0 <- per-chunk sum Re Tr[P(U[r_new]) - P(U[r_old])]
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_plaquette_delta_batch(BView<T> v, int r_old, int r_new) {
-    constexpr int NP = D * (D - 1) / 2;
-    const uint32_t n_work = v.n_chunks * NP;
-    for (uint32_t w = blockIdx.x; w < n_work; w += gridDim.x) {
-        const uint2 c = v.chunks[w / NP];
+    for (uint32_t chunk = blockIdx.x; chunk < v.n_chunks; chunk += gridDim.x) {
+        const uint2 c = v.chunks[chunk];
         const BatchEns &en = v.ens[c.x];
         const uint32_t site = c.y + threadIdx.x;
-        int mu, nu;
-        plane_dirs<D>((int)(w % NP), mu, nu);
         double r[1] = {0.0};
         if (site < en.V) {
             const int cur = v.run[c.x].cur;
             const size_t ub = (size_t)en.tile0 * (D * 9 * kTile);
-            r[0] = plaquette_delta_one<D, T, COMP>(sel_u(v, (cur + r_old) % 3) + ub, sel_u(v, (cur + r_new) % 3) + ub,
-                                                   geo_of<D>(en), site, mu, nu, v.ulo);
+            r[0] = plaquette_delta_site<D, T, COMP>(sel_u(v, (cur + r_old) % 3) + ub, sel_u(v, (cur + r_new) % 3) + ub,
+                                                    geo_of<D>(en), site, v.ulo);
         }
-        block_reduce_store<1>(r, v.partial, w, n_work);
+        block_reduce_store<1>(r, v.partial, chunk, v.n_chunks);
         __syncthreads();
     }
 }
 
-// partials[NP * n_chunks + chunk] <- per-chunk sum (e' - e)(e' + e) of E[e_old] -> E[e_new]
+// partial row 1 <- per-chunk sum (e' - e)(e' + e) of E[e_old] -> E[e_new]
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_sumsq_delta_batch(BView<T> v, int e_old, int e_new) {
     for (uint32_t chunk = blockIdx.x; chunk < v.n_chunks; chunk += gridDim.x) {
@@ -246,7 +241,7 @@ __global__ void __launch_bounds__(128) k_sumsq_delta_batch(BView<T> v, int e_old
             }
         }
         double r[1] = {(double)acc};
-        block_reduce_store<1>(r, v.partial + (size_t)(D * (D - 1) / 2) * v.n_chunks, chunk, v.n_chunks);
+        block_reduce_store<1>(r, v.partial + v.n_chunks, chunk, v.n_chunks);
         __syncthreads();
     }
 }
@@ -276,15 +271,14 @@ __global__ void __launch_bounds__(128) k_plaquette_batch(BView<T> v, int role) {
 static __global__ void __launch_bounds__(1024) k_accept_batch(const BatchEns *__restrict__ ens, BatchRun *run,
                                                        const uint64_t *__restrict__ keys,
                                                        const double *__restrict__ partial, uint32_t n_chunks,
-                                                       int n_planes, int r_final, BatchResult *results,
-                                                       int result_rows) {
+                                                       int r_final, BatchResult *results, int result_rows) {
     const int e = blockIdx.x;
     const BatchEns en = ens[e];
     double v[2] = {0.0, 0.0};
-    // the plaquette partials of an ensemble are contiguous (chunk-major, plane-minor)
-    const double *pd = partial + (size_t)en.chunk0 * n_planes;
-    for (uint32_t k = threadIdx.x; k < en.nchunks * (uint32_t)n_planes; k += blockDim.x) v[0] += pd[k];
-    for (uint32_t k = threadIdx.x; k < en.nchunks; k += blockDim.x) v[1] += partial[(size_t)n_planes * n_chunks + en.chunk0 + k];
+    for (uint32_t k = threadIdx.x; k < en.nchunks; k += blockDim.x) {
+        v[0] += partial[en.chunk0 + k];
+        v[1] += partial[n_chunks + en.chunk0 + k];
+    }
     __shared__ double res[2];
     block_reduce_store<2>(v, res, 0, 1);
     __syncthreads();
@@ -457,7 +451,7 @@ template <int D, typename T, bool COMP> struct BatchEngine {
     }
     static cudaError_t plaquette_delta(Batch &b, int r_old, int r_new) {
         k_plaquette_delta_batch<D, T, COMP>
-            <<<grid(b, BK_PLAQ_DELTA, b.n_chunks * (D * (D - 1) / 2)), kChunk, 0, b.stream>>>(view(b), r_old, r_new);
+            <<<grid(b, BK_PLAQ_DELTA, b.n_chunks), kChunk, 0, b.stream>>>(view(b), r_old, r_new);
         return cudaGetLastError();
     }
     static cudaError_t sumsq_delta(Batch &b, int e_old, int e_new) {
@@ -466,8 +460,8 @@ template <int D, typename T, bool COMP> struct BatchEngine {
         return cudaGetLastError();
     }
     static cudaError_t accept(Batch &b, int r_final) {
-        k_accept_batch<<<b.n_ens, 1024, 0, b.stream>>>(b.ens, b.run, b.keys, b.partial, b.n_chunks, D * (D - 1) / 2,
-                                                       r_final, b.results, b.result_rows);
+        k_accept_batch<<<b.n_ens, 1024, 0, b.stream>>>(b.ens, b.run, b.keys, b.partial, b.n_chunks, r_final, b.results,
+                                                       b.result_rows);
         return cudaGetLastError();
     }
     static cudaError_t plaquette(Batch &b, int role) {

@@ -141,7 +141,7 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
     static cudaError_t plaquette_delta(State &s, const void *Uold, const void *Unew, uint32_t *n_partials) {
-        const uint32_t blocks = (s.V + 127) / 128 * (D * (D - 1) / 2); // one block per 128 sites and plane
+        const uint32_t blocks = (s.V + 127) / 128;
         k_plaquette_delta<D, T, COMP>
             <<<blocks, 128, 0, s.stream>>>((const V2<T> *)Uold, (const V2<T> *)Unew, geo(s), s.partial);
         *n_partials = blocks;
@@ -205,13 +205,19 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
 
+    static cudaError_t clover_fields(State &s, const void *U, double *f_out, double *b_out) {
+        k_clover_fields<D, T><<<(s.V + 127) / 128, 128, 0, s.stream>>>((const V2<T> *)U, geo(s), f_out, b_out,
+                                                                         1.0 / (8.0 * s.size * s.size));
+        return cudaGetLastError();
+    }
+
     static const Ops *table() {
         static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
                                 efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
                                 gauss_step,     gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
                                 normalize,      finalize,       force,         link_rotate,
                                 adj_init,       adj_kick,       adj_drift,     dot,
-                                cot_links_to_aos, cot_efield_to_aos};
+                                cot_links_to_aos, cot_efield_to_aos, clover_fields};
         return &ops;
     }
 };

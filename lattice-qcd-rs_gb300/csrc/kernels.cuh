@@ -162,28 +162,21 @@ enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4, MD_EXP = 8, MD_REUNI
 //         With EXP the link moves on the group instead: U' = exp(i drift E) U, the
 //         exponential by su3_exp_i's Cayley-Hamilton recursion; REUNIT then applies
 //         orthonormalize_matrix to the result (in double, from hi + lo).
-// md_link computes link (site, mu); ulo / elo: distance in elements from a hi array to its
-// lo array (compensated storage).
+// md_update applies the kick (with the staple sum sig) and the drift to link (site, mu).  The
+// link's own values are read through ou / oul (hi / lo link) and oe / oel (hi / lo momenta), each
+// with plane stride kTile: the arrays themselves, or a copy of the block's tiles in shared memory.
 template <int D, typename T, bool COMP, int MODE>
-__device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein,
-                                        T *Eout, const Geo<D> &g, uint32_t site, int mu, T k1, T k2, T drift,
-                                        size_t ulo, size_t elo) {
-    // the staple sum first: the link and momenta of (x, mu) are loaded after it so they do
-    // not occupy registers while the neighbour links are in flight
-    mat3<T> sig;
-    if (MODE & MD_KICK) {
-        uint32_t c[D];
-        site_coords(g, site, c);
-        staple_sum<D, T>(Uin, g, site, c, mu, sig);
-    }
+__device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *ou, const V2<T> *oul, const T *oe,
+                                          const T *oel, V2<T> *__restrict__ Uout, T *Eout, bool copy_e,
+                                          uint32_t site, int mu, T k1, T k2, T drift, size_t ulo, size_t elo) {
     const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
     mat3<T> u;
-    load_mat<T>(Uin + ui, u);
+    load_mat<T>(ou, u);
     T e[8], el[8], e_old[8];
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        e[a] = Ein[ei + a * kTile];
-        el[a] = COMP ? Ein[elo + ei + a * kTile] : T(0);
+        e[a] = oe[a * kTile];
+        el[a] = COMP ? oel[a * kTile] : T(0);
         e_old[a] = e[a];
     }
     if (MODE & MD_KICK) {
@@ -202,7 +195,7 @@ __device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__
             }
             Eout[ei + a * kTile] = e[a];
         }
-    } else if (Eout != Ein) {
+    } else if (copy_e) {
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
             Eout[ei + a * kTile] = e[a];
@@ -227,7 +220,7 @@ __device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__
             for (int k = 0; k < 9; ++k) w.e[k] = cmk(-drift * x.e[k].im, drift * x.e[k].re);
         }
         mat3<T> ul;
-        if (COMP) load_mat<T>(Uin + ulo + ui, ul);
+        if (COMP) load_mat<T>(oul, ul);
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
             if (COMP) {
@@ -258,15 +251,88 @@ __device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__
         store_mat<T>(Uout + ui, u);
     }
 }
+// md_link computes link (site, mu): the staple sum first, then the link and momenta of (x, mu)
+// are loaded (after it, so they do not occupy registers while the neighbour links are in
+// flight); ulo / elo: distance in elements from a hi array to its lo array.
+template <int D, typename T, bool COMP, int MODE>
+__device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein,
+                                        T *Eout, const Geo<D> &g, uint32_t site, int mu, T k1, T k2, T drift,
+                                        size_t ulo, size_t elo) {
+    mat3<T> sig;
+    if (MODE & MD_KICK) {
+        uint32_t c[D];
+        site_coords(g, site, c);
+        staple_sum<D, T>(Uin, g, site, c, mu, sig);
+    }
+    const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
+    md_update<D, T, COMP, MODE>(sig, Uin + ui, Uin + ulo + ui, Ein + ei, Ein + elo + ei, Uout, Eout, Eout != Ein, site,
+                                mu, k1, k2, drift, ulo, elo);
+}
+
+#ifndef LQ_MD_PREFETCH
+#define LQ_MD_PREFETCH 0
+#endif
+// asynchronous 16-byte global -> shared copies (waited for with cp.async.wait_group: no spin loop)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 template <int D, typename T, bool COMP, int MODE>
 __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout,
                                   Geo<D> g, T k1, T k2, T drift) {
     const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
     const int mu = blockIdx.x % D;
-    if (site >= g.V) return;
     const size_t nt = tiles_of(g.V);
-    md_link<D, T, COMP, MODE>(Uin, Uout, Ein, Eout, g, site, mu, k1, k2, drift, nt * D * 9 * kTile,
-                              nt * D * 8 * kTile);
+    const size_t ulo = nt * D * 9 * kTile, elo = nt * D * 8 * kTile;
+#if LQ_MD_PREFETCH
+    // the block's own links and momenta (4 tiles x 9 / 8 planes of direction mu, contiguous per
+    // tile) are copied to shared memory while the staple loads are in flight
+    constexpr int NS = COMP ? 2 : 1;
+    __shared__ __align__(16) V2<T> s_u[NS][4 * 9 * kTile];
+    __shared__ __align__(16) T s_e[NS][4 * 8 * kTile];
+    {
+        const uint32_t tile0 = (blockIdx.x / D) * 4;
+        constexpr int UC = 9 * kTile * (int)sizeof(V2<T>) / 16, EC = 8 * kTile * (int)sizeof(T) / 16;
+        constexpr int per_tile = NS * (UC + EC);
+        for (int i = threadIdx.x; i < 4 * per_tile; i += blockDim.x) {
+            const int t = i / per_tile;
+            int r = i % per_tile;
+            const uint32_t tile = tile0 + (uint32_t)t;
+            if (tile >= nt) continue;
+            const int h = r / (UC + EC);
+            r %= UC + EC;
+            if (r < UC) {
+                const char *src = (const char *)(Uin + (size_t)h * ulo + ((size_t)tile * D * 9 + mu * 9) * kTile);
+                cp_async16((char *)(s_u[h] + t * 9 * kTile) + r * 16, src + r * 16);
+            } else {
+                r -= UC;
+                const char *src = (const char *)(Ein + (size_t)h * elo + ((size_t)tile * D * 8 + mu * 8) * kTile);
+                cp_async16((char *)(s_e[h] + t * 8 * kTile) + r * 16, src + r * 16);
+            }
+        }
+        cp_async_commit();
+    }
+    const bool active = site < g.V;
+    mat3<T> sig;
+    if ((MODE & MD_KICK) && active) {
+        uint32_t c[D];
+        site_coords(g, site, c);
+        staple_sum<D, T>(Uin, g, site, c, mu, sig);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (!active) return;
+    const int t = threadIdx.x / kTile, lane = threadIdx.x % kTile;
+    md_update<D, T, COMP, MODE>(sig, s_u[0] + t * 9 * kTile + lane, s_u[NS - 1] + t * 9 * kTile + lane,
+                                s_e[0] + t * 8 * kTile + lane, s_e[NS - 1] + t * 8 * kTile + lane, Uout, Eout,
+                                Eout != Ein, site, mu, k1, k2, drift, ulo, elo);
+#else
+    if (site >= g.V) return;
+    md_link<D, T, COMP, MODE>(Uin, Uout, Ein, Eout, g, site, mu, k1, k2, drift, ulo, elo);
+#endif
 }
 
 // U <- exp(i angle T^a) U for one link (finite-difference probes of the action)
@@ -583,111 +649,204 @@ __global__ void __launch_bounds__(128) k_plaquette(const V2<T> *__restrict__ U, 
 // needs only products with one difference factor, so FP32 products leave an error
 // proportional to |dU|, not to |U|.  dU = (hi' - hi) + (lo' - lo) keeps the compensated part.
 // Partial: sum Re Tr(P' - P) (Delta hamiltonian_links = -beta/3 times it).
-// planes (mu, nu), mu < nu, in the order (0,1), (0,2), ..., (D-2, D-1)
-template <int D> __device__ __forceinline__ void plane_dirs(int p, int &mu, int &nu) {
-    mu = 0;
-#pragma unroll
-    for (int m = 0; m < D - 1; ++m) {
-        const int n_in_row = D - 1 - m;
-        if (p >= n_in_row) {
-            p -= n_in_row;
-            mu = m + 1;
-        } else {
-            break;
-        }
-    }
-    nu = mu + 1 + p;
-}
-
-// Re Tr[P(U') - P(U)] of the plaquette (x; mu, nu) of one thread (see k_plaquette_delta)
 template <int D, typename T, bool COMP>
-__device__ __forceinline__ double plaquette_delta_one(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
-                                                      const Geo<D> &g, uint32_t site, int mu, int nu, size_t ulo) {
-    uint32_t c[D];
-    site_coords(g, site, c);
-    auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
-        const size_t i = tix(x, D * 9, dir * 9);
-        load_mat<T>(Uo + i, old_hi);
-        load_mat<T>(Un + i, new_hi);
-        if (COMP) {
-            mat3<T> ol, nl;
-            load_mat<T>(Uo + ulo + i, ol);
-            load_mat<T>(Un + ulo + i, nl);
+__device__ __forceinline__ double plaquette_delta_site(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
+                                                       const Geo<D> &g, uint32_t site, size_t ulo) {
+    {
+        uint32_t c[D];
+        site_coords(g, site, c);
+        auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
+            const size_t i = tix(x, D * 9, dir * 9);
+            load_mat<T>(Uo + i, old_hi);
+            load_mat<T>(Un + i, new_hi);
+            if (COMP) {
+                mat3<T> ol, nl;
+                load_mat<T>(Uo + ulo + i, ol);
+                load_mat<T>(Un + ulo + i, nl);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    diff.e[k].re = (new_hi.e[k].re - old_hi.e[k].re) + (nl.e[k].re - ol.e[k].re);
+                    diff.e[k].im = (new_hi.e[k].im - old_hi.e[k].im) + (nl.e[k].im - ol.e[k].im);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    diff.e[k].re = new_hi.e[k].re - old_hi.e[k].re;
+                    diff.e[k].im = new_hi.e[k].im - old_hi.e[k].im;
+                }
+            }
+        };
+        // Re Tr(X Y) and Re Tr(X Y^dag)
+        auto re_tr_nn = [](const mat3<T> &x, const mat3<T> &y) {
+            T s = T(0);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    s = fma(x.e[i * 3 + k].re, y.e[k * 3 + i].re, s);
+                    s = fma(-x.e[i * 3 + k].im, y.e[k * 3 + i].im, s);
+                }
+            return s;
+        };
+        auto re_tr_na = [](const mat3<T> &x, const mat3<T> &y) {
+            T s = T(0);
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                diff.e[k].re = (new_hi.e[k].re - old_hi.e[k].re) + (nl.e[k].re - ol.e[k].re);
-                diff.e[k].im = (new_hi.e[k].im - old_hi.e[k].im) + (nl.e[k].im - ol.e[k].im);
+                s = fma(x.e[k].re, y.e[k].re, s);
+                s = fma(x.e[k].im, y.e[k].im, s);
             }
-        } else {
-#pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                diff.e[k].re = new_hi.e[k].re - old_hi.e[k].re;
-                diff.e[k].im = new_hi.e[k].im - old_hi.e[k].im;
+            return s;
+        };
+        T acc = T(0);
+#pragma unroll 1
+        for (int mu = 0; mu < D; ++mu) {
+            const uint32_t xpmu = fwd(g, site, c[mu], mu);
+#pragma unroll 1
+            for (int nu = mu + 1; nu < D; ++nu) {
+                const uint32_t xpnu = fwd(g, site, c[nu], nu);
+                // links: A = U_mu(x), B = U_nu(x+mu), C = U_mu(x+nu), Dd = U_nu(x); primes: new.
+                // Evaluated in an order that keeps about four matrices live.
+                mat3<T> q1, t, s1, x_old, x_new, dx, l1;
+                T term = T(0);
+                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
+                load_mat<T>(Un + tix(xpnu, D * 9, mu * 9), t);     // C'
+                mul_nn(x_new, t, q1);                                  // Q1 = Dd' C'
+                load_mat<T>(Un + tix(xpmu, D * 9, nu * 9), t);     // B'
+                mul_na(t, q1, s1);                                     // B' C'^dag Dd'^dag
+                load_pair(mu, site, x_old, x_new, dx);                 // A, A', dA
+                term += re_tr_nn(dx, s1);                              // Tr(dA B' C'^dag Dd'^dag)
+                mul_an(q1, x_old, t);                                  // C'^dag Dd'^dag A
+                mat3<T> a_old = x_old;
+                load_pair(nu, xpmu, x_old, x_new, dx);                 // B, B', dB
+                term += re_tr_nn(dx, t);                               // Tr(A dB C'^dag Dd'^dag)
+                mul_nn(a_old, x_old, l1);                              // L1 = A B
+                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
+                mul_an(x_new, l1, t);                                  // Dd'^dag A B
+                load_pair(mu, xpnu, x_old, x_new, dx);                 // C, C', dC
+                term += re_tr_na(t, dx);                               // Tr(A B dC^dag Dd'^dag)
+                mul_na(l1, x_old, t);                                  // A B C^dag
+                load_pair(nu, site, x_old, x_new, dx);                 // Dd, Dd', dDd
+                term += re_tr_na(t, dx);                               // Tr(A B C^dag dDd^dag)
+                acc += term;
             }
         }
-    };
-    // Re Tr(X Y) and Re Tr(X Y^dag)
-    auto re_tr_nn = [](const mat3<T> &x, const mat3<T> &y) {
-        T s = T(0);
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                s = fma(x.e[i * 3 + k].re, y.e[k * 3 + i].re, s);
-                s = fma(-x.e[i * 3 + k].im, y.e[k * 3 + i].im, s);
-            }
-        return s;
-    };
-    auto re_tr_na = [](const mat3<T> &x, const mat3<T> &y) {
-        T s = T(0);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            s = fma(x.e[k].re, y.e[k].re, s);
-            s = fma(x.e[k].im, y.e[k].im, s);
-        }
-        return s;
-    };
-    const uint32_t xpmu = fwd(g, site, c[mu], mu);
-    const uint32_t xpnu = fwd(g, site, c[nu], nu);
-    // links: A = U_mu(x), B = U_nu(x+mu), C = U_mu(x+nu), Dd = U_nu(x); primes: new.
-    // Evaluated in an order that keeps about four matrices live.
-    mat3<T> q1, t, s1, x_old, x_new, dx, l1;
-    T term = T(0);
-    load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
-    load_mat<T>(Un + tix(xpnu, D * 9, mu * 9), t);     // C'
-    mul_nn(x_new, t, q1);                                  // Q1 = Dd' C'
-    load_mat<T>(Un + tix(xpmu, D * 9, nu * 9), t);     // B'
-    mul_na(t, q1, s1);                                     // B' C'^dag Dd'^dag
-    load_pair(mu, site, x_old, x_new, dx);                 // A, A', dA
-    term += re_tr_nn(dx, s1);                              // Tr(dA B' C'^dag Dd'^dag)
-    mul_an(q1, x_old, t);                                  // C'^dag Dd'^dag A
-    mat3<T> a_old = x_old;
-    load_pair(nu, xpmu, x_old, x_new, dx);                 // B, B', dB
-    term += re_tr_nn(dx, t);                               // Tr(A dB C'^dag Dd'^dag)
-    mul_nn(a_old, x_old, l1);                              // L1 = A B
-    load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
-    mul_an(x_new, l1, t);                                  // Dd'^dag A B
-    load_pair(mu, xpnu, x_old, x_new, dx);                 // C, C', dC
-    term += re_tr_na(t, dx);                               // Tr(A B dC^dag Dd'^dag)
-    mul_na(l1, x_old, t);                                  // A B C^dag
-    load_pair(nu, site, x_old, x_new, dx);                 // Dd, Dd', dDd
-    term += re_tr_na(t, dx);                               // Tr(A B C^dag dDd^dag)
-    return (double)term;
+        return (double)acc;
+    }
 }
-// One thread per plaquette: block b covers sites (b / NP) * 128 .. +127 of plane b % NP (planes
-// fastest, so the planes of a block of sites run together and share their links in L2);
-// partial b.  NP = D (D - 1) / 2.
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
                                                          Geo<D> g, double *__restrict__ partial) {
-    constexpr int NP = D * (D - 1) / 2;
-    const uint32_t site = (blockIdx.x / NP) * blockDim.x + threadIdx.x;
-    int mu, nu;
-    plane_dirs<D>((int)(blockIdx.x % NP), mu, nu);
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (site < g.V)
-        v[0] = plaquette_delta_one<D, T, COMP>(Uo, Un, g, site, mu, nu, (size_t)tiles_of(g.V) * D * 9 * kTile);
+        v[0] = plaquette_delta_site<D, T, COMP>(Uo, Un, g, site, (size_t)tiles_of(g.V) * D * 9 * kTile);
     block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
+}
+
+// ------------------------------------------------------------------ clover observables
+// Per site and plane (i < j): the clover C_ij = P_ij + P_{j,-i} + P_{-i,-j} + P_{-j,i}
+// (LinkMatrix::clover, src/field.rs:806-820; pij with U_{-mu}(x) = U_mu(x - mu)^dag), the field
+// strength F_ij = (C_ij - C_ji) / (8 size^2) = (C_ij - C_ij^dag) / (8 size^2) (f_mu_nu, :822-835; the
+// leaves of C_ji are the reversed leaves of C_ij) and the magnetic field
+// B_k = (1/2i) sum_{i,j} eps(k,i,j) F_ij = -i sum_{i<j} eps(k,i,j) F_ij (magnetic_field, :849-871,
+// with eps the three-index levi_civita of src/utils.rs:306-318).  Hi parts; double output in the
+// serde 3x3 layout: f_out[site][plane][18], b_out[site][k][18].
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_clover_fields(const V2<T> *__restrict__ U, Geo<D> g, double *f_out,
+                                                       double *b_out, double inv_8s2) {
+    constexpr int NP = D * (D - 1) / 2;
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    if (site >= g.V) return;
+    uint32_t c[D];
+    site_coords(g, site, c);
+    auto ld = [&](uint32_t x, int dir, mat3<T> &m) { load_mat<T>(U + tix(x, D * 9, dir * 9), m); };
+    auto store18 = [](double *dst, const mat3<double> &m) {
+#pragma unroll
+        for (int col = 0; col < 3; ++col)
+#pragma unroll
+            for (int row = 0; row < 3; ++row) {
+                dst[(col * 3 + row) * 2] = m.e[row * 3 + col].re;
+                dst[(col * 3 + row) * 2 + 1] = m.e[row * 3 + col].im;
+            }
+    };
+    // B accumulates in its output rows (each thread owns its site's rows)
+    if (b_out)
+        for (int q = 0; q < D * 18; ++q) b_out[(size_t)site * D * 18 + q] = 0.0;
+    int p = 0;
+#pragma unroll 1
+    for (int i = 0; i < D; ++i) {
+#pragma unroll 1
+        for (int j = i + 1; j < D; ++j, ++p) {
+            const uint32_t xpi = fwd(g, site, c[i], i), xmi = bwd(g, site, c[i], i);
+            const uint32_t xpj = fwd(g, site, c[j], j), xmj = bwd(g, site, c[j], j);
+            const uint32_t xpj_mi = bwd(g, xpj, c[i], i), xmi_mj = bwd(g, xmi, c[j], j);
+            const uint32_t xpi_mj = bwd(g, xpi, c[j], j);
+            mat3<T> a, bb, t1, t2, leaf, cl;
+            // P_ij = U_i(x) U_j(x+i) U_i(x+j)^dag U_j(x)^dag
+            ld(site, i, a);
+            ld(xpi, j, bb);
+            mul_nn(a, bb, t1);
+            ld(xpj, i, a);
+            mul_na(t1, a, t2);
+            ld(site, j, a);
+            mul_na(t2, a, cl);
+            // P_{j,-i} = U_j(x) U_i(x+j-i)^dag U_j(x-i)^dag U_i(x-i)
+            ld(site, j, a);
+            ld(xpj_mi, i, bb);
+            mul_na(a, bb, t1);
+            ld(xmi, j, a);
+            mul_na(t1, a, t2);
+            ld(xmi, i, a);
+            mul_nn(t2, a, leaf);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) cl.e[k] = cmk(cl.e[k].re + leaf.e[k].re, cl.e[k].im + leaf.e[k].im);
+            // P_{-i,-j} = U_i(x-i)^dag U_j(x-i-j)^dag U_i(x-i-j) U_j(x-j)
+            ld(xmi_mj, j, a);
+            ld(xmi, i, bb);
+            mul_nn(a, bb, t1); // (U_i(x-i)^dag U_j(x-i-j)^dag)^dag
+            ld(xmi_mj, i, a);
+            mul_an(t1, a, t2);
+            ld(xmj, j, a);
+            mul_nn(t2, a, leaf);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) cl.e[k] = cmk(cl.e[k].re + leaf.e[k].re, cl.e[k].im + leaf.e[k].im);
+            // P_{-j,i} = U_j(x-j)^dag U_i(x-j) U_j(x+i-j) U_i(x)^dag
+            ld(xmj, j, a);
+            ld(xmj, i, bb);
+            mul_an(a, bb, t1);
+            ld(xpi_mj, j, a);
+            mul_nn(t1, a, t2);
+            ld(site, i, a);
+            mul_na(t2, a, leaf);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) cl.e[k] = cmk(cl.e[k].re + leaf.e[k].re, cl.e[k].im + leaf.e[k].im);
+            // F_ij = (C - C^dag) / (8 size^2), in double
+            mat3<double> f;
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const cpx<T> x = cl.e[r * 3 + q], y = cl.e[q * 3 + r];
+                    f.e[r * 3 + q] = cmk(((double)x.re - (double)y.re) * inv_8s2, ((double)x.im + (double)y.im) * inv_8s2);
+                }
+            if (f_out) store18(f_out + ((size_t)site * NP + p) * 18, f);
+            // B_k += -i eps(k, i, j) F_ij: -i (a + ib) = b - ia
+            if (b_out)
+                for (int k = 0; k < D; ++k) {
+                    if (k == i || k == j) continue;
+                    const double eps = (double)(((i > k) - (i < k)) * ((j > k) - (j < k)) * ((j > i) - (j < i)));
+                    double *dst = b_out + ((size_t)site * D + k) * 18;
+#pragma unroll
+                    for (int col = 0; col < 3; ++col)
+#pragma unroll
+                        for (int row = 0; row < 3; ++row) {
+                            const cpx<double> x = f.e[row * 3 + col];
+                            dst[(col * 3 + row) * 2] += eps * x.im;
+                            dst[(col * 3 + row) * 2 + 1] -= eps * x.re;
+                        }
+                }
+        }
+    }
 }
 
 // sum of squares of an E-field (hi + lo), hamiltonian_efield before the beta/2 factor

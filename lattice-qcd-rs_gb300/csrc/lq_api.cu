@@ -584,6 +584,26 @@ int lq_gauss_download(lq_state *s, double *out, size_t n_doubles) {
     return LQ_OK;
 }
 
+// ------------------------------------------------------------------ clover observables
+namespace {
+int clover_download(lq_state *s, double *out, size_t n, bool magnetic) {
+    LQ_CHECK_STATE(s);
+    if (!out) return LQ_ERR_INVALID_ARGUMENT;
+    const size_t per_site = magnetic ? (size_t)s->dim : (size_t)(s->dim * (s->dim - 1) / 2);
+    if (n != (size_t)s->V * per_site * 18) return LQ_ERR_INCOMPATIBLE_SIZE;
+    int rc = ensure_staging(*s, n * sizeof(double));
+    if (rc) return rc;
+    double *d = (double *)s->staging;
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->clover_fields(*s, s->U[s->cur], magnetic ? nullptr : d, magnetic ? d : nullptr));
+    LQ_CK(cudaMemcpyAsync(out, d, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    LQ_CK(sync_stream(*s));
+    return LQ_OK;
+}
+} // namespace
+
+int lq_field_strength(lq_state *s, double *out, size_t n_doubles) { return clover_download(s, out, n_doubles, false); }
+int lq_magnetic_field(lq_state *s, double *out, size_t n_doubles) { return clover_download(s, out, n_doubles, true); }
+
 // ------------------------------------------------------------------ differentiation
 int lq_wilson_action(lq_state *s, double *out) { return lq_hamiltonian_links(s, out); }
 

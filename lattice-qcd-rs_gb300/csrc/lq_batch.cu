@@ -406,7 +406,7 @@ int lq_batch_create(int dim, int n_ensembles, const int *L, const double *size, 
     alloc((void **)&b->run, sizeof(lq::BatchRun) * n_ensembles, __LINE__);
     alloc((void **)&b->chunks, sizeof(uint2) * chunks, __LINE__);
     alloc((void **)&b->keys, sizeof(uint64_t) * n_ensembles, __LINE__);
-    alloc((void **)&b->partial, sizeof(double) * lq::batch_partial_rows(dim) * chunks, __LINE__);
+    alloc((void **)&b->partial, sizeof(double) * 3 * chunks, __LINE__);
     alloc((void **)&b->done, sizeof(unsigned int), __LINE__);
     alloc((void **)&b->flag, sizeof(int), __LINE__);
     if (!rc) {
@@ -425,7 +425,7 @@ int lq_batch_create(int dim, int n_ensembles, const int *L, const double *size, 
             if (e == cudaSuccess) e = cudaMemsetAsync(b->G[i], 0, b->gauss_bytes(), b->stream);
         }
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(b->partial, 0, sizeof(double) * lq::batch_partial_rows(dim) * chunks, b->stream);
+            e = cudaMemsetAsync(b->partial, 0, sizeof(double) * 3 * chunks, b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(b->done, 0, sizeof(unsigned int), b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(b->flag, 0, sizeof(int), b->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
@@ -477,7 +477,7 @@ int lq_batch_info(const lq_batch *b, int *dim, int *n_ensembles, long long *tota
     if (total_links) *total_links = (long long)b->total_links;
     if (device_bytes)
         *device_bytes = 3 * b->link_bytes() + 2 * b->efield_bytes() + 2 * b->gauss_bytes() +
-                        sizeof(double) * lq::batch_partial_rows(b->dim) * (size_t)b->n_chunks +
+                        sizeof(double) * 3 * (size_t)b->n_chunks +
                         sizeof(uint2) * (size_t)b->n_chunks +
                         (sizeof(lq::BatchEns) + sizeof(lq::BatchRun) + 8) * (size_t)b->n_ens;
     return LQ_OK;
@@ -590,10 +590,7 @@ int lq_batch_autotune(lq_batch *b, double dt, int reps) {
     BK(b->ops->gauss(*b, 0, 0));
     for (int cls = 0; cls < lq::BK_CLASSES; ++cls) {
         const bool per_link = cls == lq::BK_MD || cls == lq::BK_NORMAL;
-        const uint32_t per_chunk = per_link ? (uint32_t)b->dim
-                                   : cls == lq::BK_PLAQ_DELTA ? (uint32_t)(b->dim * (b->dim - 1) / 2)
-                                                                : 1u;
-        const uint32_t n_work = b->n_chunks * per_chunk;
+        const uint32_t n_work = b->n_chunks * (per_link ? (uint32_t)b->dim : 1u);
         const int occ = b->ops->occupancy(cls);
         std::vector<uint32_t> grids = {0};
         if (occ > 0)

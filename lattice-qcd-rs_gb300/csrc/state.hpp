@@ -116,16 +116,17 @@ struct Ops {
     cudaError_t (*dot)(State &s, const void *a, const void *b, uint32_t *n_partials);
     cudaError_t (*cot_links_to_aos)(State &s, const void *lamU, double *d_aos);
     cudaError_t (*cot_efield_to_aos)(State &s, const void *lamE, double *d_aos);
+    // clover field strength F_ij (i < j) and magnetic field per site, double, serde 3x3 layout
+    cudaError_t (*clover_fields)(State &s, const void *U, double *f_out, double *b_out);
 };
 
 const Ops *ops_f64(int dim);
 const Ops *ops_f32(int dim);
 const Ops *ops_mixed(int dim);
 
-// partial slots needed for V sites (per row), and the rows of the partial buffer: the plaquette
-// difference keeps one partial per 128 sites and plane, D (D - 1) / 2 <= 6 planes
+// partial slots needed for V sites (per row), and the rows of the partial buffer
 inline uint32_t partial_slots_for(uint32_t V) { return (V + 127) / 128 + 64; }
-constexpr int kPartialRows = 6;
+constexpr int kPartialRows = 3;
 
 } // namespace lq
 

@@ -78,6 +78,8 @@ SIGNATURES = {
     "lq_wilson_action": (_i32, [_vp, _dp]),
     "lq_wilson_action_backward": (_i32, [_vp, _dp, _sz]),
     "lq_link_rotate": (_i32, [_vp, ctypes.c_longlong, _i32, _f64]),
+    "lq_field_strength": (_i32, [_vp, _dp, _sz]),
+    "lq_magnetic_field": (_i32, [_vp, _dp, _sz]),
     "lq_leapfrog_adjoint": (_i32, [_vp, _f64, _i32, _i32, _dp, _dp, _dp, _sz, _dp, _sz, _szp]),
     "lq_profile_enable": (_i32, [_vp, _i32]),
     "lq_profile_read": (_i32, [_vp, _i32, _llp, _dp, _i32]),
@@ -285,6 +287,18 @@ class State:
         _check(load().lq_link_rotate(self._h, link, generator, angle), "lq_link_rotate")
 
     # ---- updates
+    def field_strength(self):
+        """F_ij (clover) at every site for the planes i < j: float64[V, D(D-1)/2, 18]"""
+        out = np.empty((self.L ** self.dim, self.dim * (self.dim - 1) // 2, 18))
+        _check(load().lq_field_strength(self._h, _p(out), out.size), "lq_field_strength")
+        return out
+
+    def magnetic_field(self):
+        """magnetic_field_vec at every site: float64[V, D, 18]"""
+        out = np.empty((self.L ** self.dim, self.dim, 18))
+        _check(load().lq_magnetic_field(self._h, _p(out), out.size), "lq_magnetic_field")
+        return out
+
     def leapfrog_adjoint(self, dt, n_steps, checkpoint_every=0, grads=True):
         """O = <Re Tr P>/3 after n_steps symplectic steps, dO/dbeta (momenta scaled as 1/beta) and,
         with grads, dO/dU0 (complex cotangent per link, serde layout) and dO/dE0."""

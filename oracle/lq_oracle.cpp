@@ -435,6 +435,47 @@ inline M3 pij(const Lattice &lat, const double *links, long site, Dir di, Dir dj
     return u_i * adjoint(s);
 }
 
+/* clover, src/field.rs:806-820: C_ij = P_ij + P_{j,-i} + P_{-i,-j} + P_{-j,i} */
+inline M3 clover(const Lattice &lat, const double *links, long site, Dir di, Dir dj) {
+    const Dir mi{di.index, !di.positive}, mj{dj.index, !dj.positive};
+    return ((pij(lat, links, site, di, dj) + pij(lat, links, site, dj, mi)) + pij(lat, links, site, mi, mj)) +
+           pij(lat, links, site, mj, di);
+}
+/* complex division as num-complex divides: (a + ib) / (c + id) = ((ac + bd) + i(bc - ad)) / (c^2 + d^2) */
+inline M3 div_cx(const M3 &m, Cx c) {
+    const double n = c.re * c.re + c.im * c.im;
+    M3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const Cx a = m.m[i][j];
+            r.m[i][j] = Cx{(a.re * c.re + a.im * c.im) / n, (a.im * c.re - a.re * c.im) / n};
+        }
+    return r;
+}
+/* f_mu_nu, src/field.rs:822-835: (C_ij - C_ji) / (8 size^2) */
+inline M3 f_mu_nu(const Lattice &lat, double size, const double *links, long site, Dir di, Dir dj) {
+    const M3 m = clover(lat, links, site, di, dj) - clover(lat, links, site, dj, di);
+    return div_cx(m, cx(8.0 * size * size));
+}
+/* levi_civita, src/utils.rs:306-318: product over i > j of sign(index[i] - index[j]) */
+inline int levi_civita3(int a, int b, int c) {
+    auto sg = [](int x, int y) { return x > y ? 1 : (x < y ? -1 : 0); };
+    return sg(b, a) * sg(c, a) * sg(c, b);
+}
+/* magnetic_field, src/field.rs:849-871: sum_i sum_j eps(k, i, j) F_ij / (2i), positive directions */
+inline M3 magnetic_field(const Lattice &lat, double size, const double *links, long site, int k) {
+    M3 sum = zero3();
+    for (int i = 0; i < lat.D; ++i) {
+        M3 inner = zero3();
+        for (int j = 0; j < lat.D; ++j) {
+            const M3 f = f_mu_nu(lat, size, links, site, Dir{i, true}, Dir{j, true});
+            inner = inner + f * cx((double)levi_civita3(k, i, j));
+        }
+        sum = sum + inner;
+    }
+    return div_cx(sum, Cx{0.0, 2.0});
+}
+
 /* Direction::directions(): [+0, -0, +1, -1, ...], procedural_macro/src/lib.rs:53-83 */
 inline Dir direction_at(int k) { return Dir{k / 2, (k % 2) == 0}; }
 
@@ -779,6 +820,31 @@ int or_average_trace_plaquette(int dim, int L, const double *links, double *re, 
     const double n_plaq = (double)(lat.V * ((dim * (dim - 1)) / 2));
     *re = sre / n_plaq;
     *im = sim / n_plaq;
+    return OR_OK;
+}
+/* clover / f_mu_nu / magnetic_field at one point (signed directions: index, positive flag) */
+int or_clover(int dim, int L, const double *links, long site, int i, int i_pos, int j, int j_pos, double *out18) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    if (site < 0 || site >= lat.V || i < 0 || i >= dim || j < 0 || j >= dim) return OR_ERR_INVALID_ARGUMENT;
+    store_m3(clover(lat, links, site, Dir{i, i_pos != 0}, Dir{j, j_pos != 0}), out18);
+    return OR_OK;
+}
+int or_f_mu_nu(int dim, int L, double size, const double *links, long site, int i, int j, double *out18) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    if (site < 0 || site >= lat.V || i < 0 || i >= dim || j < 0 || j >= dim) return OR_ERR_INVALID_ARGUMENT;
+    store_m3(f_mu_nu(lat, size, links, site, Dir{i, true}, Dir{j, true}), out18);
+    return OR_OK;
+}
+int or_magnetic_field(int dim, int L, double size, const double *links, long site, int k, double *out18) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    const Lattice lat(dim, L);
+    if (site < 0 || site >= lat.V || k < 0 || k >= dim) return OR_ERR_INVALID_ARGUMENT;
+    store_m3(magnetic_field(lat, size, links, site, k), out18);
     return OR_OK;
 }
 int or_gauss(int dim, int L, const double *links, const double *efield, long site, double *out18) {

@@ -76,6 +76,10 @@ int or_efield_normal(int dim, int L, void *rng, double std_dev, double *efield);
 int or_hamiltonian_links(int dim, int L, double beta, const double *links, double *out);
 int or_hamiltonian_efield(int dim, int L, double beta, const double *efield, double *out);
 int or_average_trace_plaquette(int dim, int L, const double *links, double *re, double *im);
+/* LinkMatrix::clover / f_mu_nu / magnetic_field (src/field.rs:806-871) at one point */
+int or_clover(int dim, int L, const double *links, long site, int i, int i_pos, int j, int j_pos, double *out18);
+int or_f_mu_nu(int dim, int L, double size, const double *links, long site, int i, int j, double *out18);
+int or_magnetic_field(int dim, int L, double size, const double *links, long site, int k, double *out18);
 int or_gauss(int dim, int L, const double *links, const double *efield, long site, double *out18);
 int or_gauss_sum_div(int dim, int L, const double *links, const double *efield, double *out);
 int or_project_to_gauss(int dim, int L, const double *links, const double *efield_in,

@@ -67,6 +67,9 @@ def lib():
             "or_hamiltonian_efield": (i32, [i32, i32, f64, _dp, _dp]),
             "or_average_trace_plaquette": (i32, [i32, i32, _dp, _dp, _dp]),
             "or_gauss": (i32, [i32, i32, _dp, _dp, lng, _dp]),
+            "or_clover": (i32, [i32, i32, _dp, lng, i32, i32, i32, i32, _dp]),
+            "or_f_mu_nu": (i32, [i32, i32, ctypes.c_double, _dp, lng, i32, i32, _dp]),
+            "or_magnetic_field": (i32, [i32, i32, ctypes.c_double, _dp, lng, i32, _dp]),
             "or_gauss_sum_div": (i32, [i32, i32, _dp, _dp, _dp]),
             "or_project_to_gauss": (i32, [i32, i32, _dp, _dp, _dp, i32, ip]),
             "or_normalize": (i32, [i32, i32, _dp]),
@@ -223,6 +226,27 @@ def average_trace_plaquette(dim, L, links):
 def gauss(dim, L, links, efield, site):
     out = np.zeros(18)
     _check(lib().or_gauss(dim, L, _p(links), _p(efield), site, _p(out)), "gauss")
+    return out
+
+
+def clover(dim, L, links, site, i, j, i_positive=True, j_positive=True):
+    """LinkMatrix::clover (src/field.rs:806-820) at one point, 18 doubles"""
+    out = np.zeros(18)
+    _check(lib().or_clover(dim, L, _p(links), site, i, int(i_positive), j, int(j_positive), _p(out)), "clover")
+    return out
+
+
+def f_mu_nu(dim, L, size, links, site, i, j):
+    """LinkMatrix::f_mu_nu (src/field.rs:822-835), positive directions"""
+    out = np.zeros(18)
+    _check(lib().or_f_mu_nu(dim, L, size, _p(links), site, i, j, _p(out)), "f_mu_nu")
+    return out
+
+
+def magnetic_field(dim, L, size, links, site, k):
+    """LinkMatrix::magnetic_field (src/field.rs:849-871) along positive direction k"""
+    out = np.zeros(18)
+    _check(lib().or_magnetic_field(dim, L, size, _p(links), site, k, _p(out)), "magnetic_field")
     return out
 
 

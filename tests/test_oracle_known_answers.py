@@ -249,3 +249,38 @@ def test_nan_momentum_is_gauss_projection_error(oracle_mod):
     with pytest.raises(O.OracleError) as ei:
         O.project_to_gauss(dim, L, links, e)
     assert ei.value.code == O.OR_ERR_GAUSS_PROJECTION
+
+
+def test_clover_and_magnetic_field_known_answers(oracle_mod):
+    """The reference's magnetic_field test (src/field.rs:1579-1711): D = 3, L = 4, size 1."""
+    O = oracle_mod
+    dim, L, size = 3, 4, 1.0
+    I3 = np.eye(3)
+
+    def close(m18, expect):
+        return np.abs(O.to_complex(m18) - expect).max() <= 1e-15
+
+    links = O.links_cold(dim, L)
+    assert close(O.clover(dim, L, links, 0, 0, 1), 4 * I3)
+    assert close(O.f_mu_nu(dim, L, size, links, 0, 0, 1), 0 * I3)
+    for k in range(3):
+        assert close(O.magnetic_field(dim, L, size, links, 0, k), 0 * I3)
+    # link 0 (site 0, direction x) = i 1
+    links[0] = O.from_complex(1j * I3)
+    assert close(O.clover(dim, L, links, 0, 0, 1), 2 * I3)
+    assert close(O.clover(dim, L, links, 0, 1, 0), 2 * I3)
+    assert close(O.f_mu_nu(dim, L, size, links, 0, 0, 1), 0 * I3)
+    for k in range(3):
+        assert close(O.magnetic_field(dim, L, size, links, 0, k), 0 * I3)
+    # cold again, link (site [1, 0, 0], direction y) = i 1: link index = site * D + mu = 1 * 3 + 1
+    links = O.links_cold(dim, L)
+    links[1 * dim + 1] = O.from_complex(1j * I3)
+    assert close(O.clover(dim, L, links, 0, 0, 1), (3 + 1j) * I3)
+    assert close(O.clover(dim, L, links, 0, 1, 0), (3 - 1j) * I3)
+    assert close(O.f_mu_nu(dim, L, size, links, 0, 0, 1), 0.25j * I3)
+    assert close(O.magnetic_field(dim, L, size, links, 0, 0), 0 * I3)
+    assert close(O.magnetic_field(dim, L, size, links, 0, 2), 0.25 * I3)
+    assert close(O.magnetic_field(dim, L, size, links, 0, 1), 0 * I3)
+    # the point [4, 0, 0] wraps to [0, 0, 0]
+    b = O.magnetic_field(dim, L, size, links, 0, 2)
+    assert np.array_equal(b, O.magnetic_field(dim, L, size, links, 4 % L, 2))

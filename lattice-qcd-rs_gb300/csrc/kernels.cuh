@@ -269,17 +269,6 @@ __device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__
                                 mu, k1, k2, drift, ulo, elo);
 }
 
-#ifndef LQ_MD_PREFETCH
-#define LQ_MD_PREFETCH 0
-#endif
-// asynchronous 16-byte global -> shared copies (waited for with cp.async.wait_group: no spin loop)
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
 template <int D, typename T, bool COMP, int MODE>
 __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout,
                                   Geo<D> g, T k1, T k2, T drift) {
@@ -287,52 +276,8 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
     const int mu = blockIdx.x % D;
     const size_t nt = tiles_of(g.V);
     const size_t ulo = nt * D * 9 * kTile, elo = nt * D * 8 * kTile;
-#if LQ_MD_PREFETCH
-    // the block's own links and momenta (4 tiles x 9 / 8 planes of direction mu, contiguous per
-    // tile) are copied to shared memory while the staple loads are in flight
-    constexpr int NS = COMP ? 2 : 1;
-    __shared__ __align__(16) V2<T> s_u[NS][4 * 9 * kTile];
-    __shared__ __align__(16) T s_e[NS][4 * 8 * kTile];
-    {
-        const uint32_t tile0 = (blockIdx.x / D) * 4;
-        constexpr int UC = 9 * kTile * (int)sizeof(V2<T>) / 16, EC = 8 * kTile * (int)sizeof(T) / 16;
-        constexpr int per_tile = NS * (UC + EC);
-        for (int i = threadIdx.x; i < 4 * per_tile; i += blockDim.x) {
-            const int t = i / per_tile;
-            int r = i % per_tile;
-            const uint32_t tile = tile0 + (uint32_t)t;
-            if (tile >= nt) continue;
-            const int h = r / (UC + EC);
-            r %= UC + EC;
-            if (r < UC) {
-                const char *src = (const char *)(Uin + (size_t)h * ulo + ((size_t)tile * D * 9 + mu * 9) * kTile);
-                cp_async16((char *)(s_u[h] + t * 9 * kTile) + r * 16, src + r * 16);
-            } else {
-                r -= UC;
-                const char *src = (const char *)(Ein + (size_t)h * elo + ((size_t)tile * D * 8 + mu * 8) * kTile);
-                cp_async16((char *)(s_e[h] + t * 8 * kTile) + r * 16, src + r * 16);
-            }
-        }
-        cp_async_commit();
-    }
-    const bool active = site < g.V;
-    mat3<T> sig;
-    if ((MODE & MD_KICK) && active) {
-        uint32_t c[D];
-        site_coords(g, site, c);
-        staple_sum<D, T>(Uin, g, site, c, mu, sig);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    if (!active) return;
-    const int t = threadIdx.x / kTile, lane = threadIdx.x % kTile;
-    md_update<D, T, COMP, MODE>(sig, s_u[0] + t * 9 * kTile + lane, s_u[NS - 1] + t * 9 * kTile + lane,
-                                s_e[0] + t * 8 * kTile + lane, s_e[NS - 1] + t * 8 * kTile + lane, Uout, Eout,
-                                Eout != Ein, site, mu, k1, k2, drift, ulo, elo);
-#else
     if (site >= g.V) return;
     md_link<D, T, COMP, MODE>(Uin, Uout, Ein, Eout, g, site, mu, k1, k2, drift, ulo, elo);
-#endif
 }
 
 // U <- exp(i angle T^a) U for one link (finite-difference probes of the action)

@@ -237,6 +237,19 @@ template <int D> class LatticeStateDefault {
         if (lq_average_trace_plaquette(raw(), &re, &im) != LQ_OK) return std::nullopt;
         return Complex(re, im);
     }
+    // LinkMatrix::f_mu_nu at every point for the planes i < j (src/field.rs:822-835), computed on the
+    // device: [site][plane][18], planes in the order (0,1), (0,2), ..., (D-2,D-1)
+    std::vector<double> field_strength() const {
+        std::vector<double> out(lattice_.number_of_points() * (std::size_t)(D * (D - 1) / 2) * 18);
+        check(lq_field_strength(raw(), out.data(), out.size()), "lq_field_strength");
+        return out;
+    }
+    // LinkMatrix::magnetic_field_vec at every point (src/field.rs:837-871): [site][k][18]
+    std::vector<double> magnetic_field() const {
+        std::vector<double> out(lattice_.number_of_points() * (std::size_t)D * 18);
+        check(lq_magnetic_field(raw(), out.data(), out.size()), "lq_magnetic_field");
+        return out;
+    }
     // LatticeStateDefault::normalize_link_matrices (src/simulation/state.rs:754-756)
     void normalize_link_matrices() {
         check(lq_normalize_link_matrices(raw()), "lq_normalize_link_matrices");

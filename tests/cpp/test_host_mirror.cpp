@@ -95,6 +95,19 @@ int main() {
         CHECK(std::fabs(fd - g.data[(std::size_t)link * 8 + a]) < 1e-4);
     }
 
+    // clover observables on a cold lattice: F = 0 and B = 0 (src/field.rs:1579-1600)
+    {
+        auto cold = LatticeStateDefault<3>::new_cold(1.0, 1.0, 4).unwrap();
+        const auto f = cold.field_strength();
+        const auto b = cold.magnetic_field();
+        CHECK(f.size() == 64u * 3 * 18);
+        CHECK(b.size() == 64u * 3 * 18);
+        double worst = 0.0;
+        for (double x : f) worst = std::fmax(worst, std::fabs(x));
+        for (double x : b) worst = std::fmax(worst, std::fabs(x));
+        CHECK(worst == 0.0);
+    }
+
     // setter with a wrong size panics, as the reference's set_link_matrix does
     {
         auto s = LatticeStateDefault<2>::new_cold(1.0, 1.0, 4).unwrap();

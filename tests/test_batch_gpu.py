@@ -142,3 +142,30 @@ def test_uneven_batch_dims_2_and_3(lqgpu_mod):
                     r = s.hmc_trajectory(0.02, 4, 11 + e, k, float(res["uniform"][k, e]), MAXG)
                     assert r["accepted"] == res["accepted"][k, e]
                 assert np.array_equal(s.link_matrix(), links[e])
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_tiny_and_ragged_ensembles(lqgpu_mod, precision):
+    """L = 2 (x + mu and x - mu coincide) and volumes that end inside a tile (3^4 = 81, 5^4 = 625
+    sites) next to each other in one batch; a batch of one ensemble."""
+    G = lqgpu_mod
+    for Ls, betas in (([2, 3, 2, 5], [2.0, 3.0, 4.0, 2.5]), ([3], [2.0])):
+        n = len(Ls)
+        with G.Batch(DIM, Ls, [1000.0] * n, betas, precision) as b:
+            b.set_links_random(21)
+            b.set_seed(5, 0)
+            b.hmc_run(DT, 4, 2, MAXG)
+            res = b.hmc_results()
+            links = [b.link_matrix(e) for e in range(n)]
+        assert (res["status"] == 0).all()
+        for e, (L, beta) in enumerate(zip(Ls, betas)):
+            with G.State(DIM, L, 1000.0, beta, precision) as s:
+                s.set_links_random(21 + e)
+                for k in range(2):
+                    r = s.hmc_trajectory(DT, 4, 5 + e, k, float(res["uniform"][k, e]), MAXG)
+                    assert r["accepted"] == res["accepted"][k, e]
+                    assert r["gauss_steps"] == res["gauss_steps"][k, e]
+                if precision == 0:
+                    assert np.abs(s.link_matrix() - links[e]).max() <= 1e-12
+                else:
+                    assert np.array_equal(s.link_matrix(), links[e])

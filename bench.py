@@ -204,10 +204,10 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU arm
-# DRAM bytes (read + write) per link of one k_md kick+drift launch, from one ncu capture at 28^4
-# (profiles/k_md_mixed_28x4.md: 994.1 MB for 2,458,624 links); traffic scales with the links of
-# a launch, so the full-size value is this times the links.
-NCU_MD_TRAFFIC_PER_LINK = {"mixed": 994.1e6 / 2458624}
+# DRAM bytes (read + write) per link of one k_md kick+drift launch, from one ncu capture of the
+# mixed kernel at 28^4 (995.1 MB for 2,458,624 links); traffic scales with the links of a launch,
+# so the full-size value is this times the links.
+NCU_MD_TRAFFIC_PER_LINK = {"mixed": 995.1e6 / 2458624}
 
 
 def algorithmic_md_bytes(n_links, md_steps, real_bytes):

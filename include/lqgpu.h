@@ -172,6 +172,21 @@ int lq_integrate(lq_state *s, int mode, double dt, int n);
 /* simulate_using_leapfrog_n (src/simulation/state.rs:318-357) */
 int lq_leapfrog_n(lq_state *s, double dt, int n);
 
+/* ---------------------------------------------------------------- local Monte Carlo sweeps
+ * MetropolisHastingsSweep::next_element (src/simulation/monte_carlo/metropolis_hastings_sweep.rs:147-177,
+ * proposals new = prod_k orthonormalize(random_su3_close_to_unity(spread)) U, accepted with
+ * min(1, exp(-Delta S)), Delta S = -Re Tr((U' - U) A) beta / 3 with the staple A of mod.rs:339-362) and
+ * HeatBathSweep::next_element (heat_bath.rs:88-121, the pseudo heat bath on the three SU(2)
+ * subgroups).  One call is one sweep over every link, in checkerboard order (for each direction,
+ * the links on even sites, then on odd sites) instead of the reference's lattice order, so L must be
+ * even (else LQ_ERR_INVALID_ARGUMENT).  Random numbers: a Philox4x32-10 stream per link keyed by seed,
+ * counter = sweep (not the rand crate's streams).  lq_metropolis_sweep returns the number of accepted
+ * updates and the mean acceptance probability (number_replace_last, prob_replace_mean); its argument
+ * checks are MetropolisHastingsSweep::new's (n_update >= 1, 0 < spread < 1). */
+int lq_metropolis_sweep(lq_state *s, int n_update, double spread, uint64_t seed, uint64_t sweep,
+                        long long *n_accepted, double *prob_mean);
+int lq_heat_bath_sweep(lq_state *s, uint64_t seed, uint64_t sweep);
+
 /* ---------------------------------------------------------------- clover observables
  * LinkMatrix::f_mu_nu and magnetic_field_vec (src/field.rs:822-871) at every site, from the clover
  * C_ij = P_ij + P_{j,-i} + P_{-i,-j} + P_{-j,i} (src/field.rs:806-820):

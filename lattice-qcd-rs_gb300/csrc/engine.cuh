@@ -5,6 +5,7 @@
 #include "adjoint.cuh"
 #include "kernels.cuh"
 #include "state.hpp"
+#include "sweeps.cuh"
 
 namespace lq {
 
@@ -211,13 +212,31 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
 
+    // one checkerboard class of a Metropolis (alg 0) or heat-bath (alg 1) sweep on U in place;
+    // Metropolis partials (2 rows) in s.partial, their count in *n_partials
+    static cudaError_t mc_sweep(State &s, void *U, int alg, int mu, int parity, double beta, uint64_t seed,
+                                uint64_t sweep, int n_update, double spread, uint32_t *n_partials) {
+        const uint32_t blocks = (s.V + 127) / 128;
+        const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+        if (alg == MC_METROPOLIS)
+            k_mc_sweep<D, T, COMP, MC_METROPOLIS><<<blocks, 128, 0, s.stream>>>(
+                (V2<T> *)U, geo(s), mu, parity, beta, key, (uint32_t)sweep, (uint32_t)(sweep >> 32), n_update, spread,
+                s.partial);
+        else
+            k_mc_sweep<D, T, COMP, MC_HEAT_BATH><<<blocks, 128, 0, s.stream>>>(
+                (V2<T> *)U, geo(s), mu, parity, beta, key, (uint32_t)sweep, (uint32_t)(sweep >> 32), n_update, spread,
+                s.partial);
+        *n_partials = blocks;
+        return cudaGetLastError();
+    }
+
     static const Ops *table() {
         static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
                                 efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
                                 gauss_step,     gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
                                 normalize,      finalize,       force,         link_rotate,
                                 adj_init,       adj_kick,       adj_drift,     dot,
-                                cot_links_to_aos, cot_efield_to_aos, clover_fields};
+                                cot_links_to_aos, cot_efield_to_aos, clover_fields, mc_sweep};
         return &ops;
     }
 };

@@ -14,6 +14,7 @@
 #include "kernels.cuh"
 #include "lqgpu.h"
 #include "state.hpp"
+#include "sweeps.cuh"
 
 using lq::State;
 
@@ -603,6 +604,55 @@ int clover_download(lq_state *s, double *out, size_t n, bool magnetic) {
 
 int lq_field_strength(lq_state *s, double *out, size_t n_doubles) { return clover_download(s, out, n_doubles, false); }
 int lq_magnetic_field(lq_state *s, double *out, size_t n_doubles) { return clover_download(s, out, n_doubles, true); }
+
+// ------------------------------------------------------------------ local Monte Carlo sweeps
+namespace {
+int mc_sweep(lq_state *s, int alg, int n_update, double spread, uint64_t seed, uint64_t sweep,
+             long long *n_accepted, double *prob_mean) {
+    LQ_CHECK_STATE(s);
+    if (s->L % 2 != 0) {
+        lq::set_last_error("checkerboard sweeps need an even number of points per direction");
+        return LQ_ERR_INVALID_ARGUMENT;
+    }
+    if (s->leap) return LQ_ERR_WRONG_STATE_KIND;
+    State &st = *s;
+    state_changed(st);
+    double acc = 0.0, psum = 0.0;
+    for (int mu = 0; mu < st.dim; ++mu)
+        for (int parity = 0; parity < 2; ++parity) {
+            uint32_t n = 0;
+            LQ_LAUNCH(st, LQ_KERNEL_OTHER,
+                      st.ops->mc_sweep(st, st.U[st.cur], alg, mu, parity, st.beta, seed, sweep, n_update, spread, &n));
+            if (alg == lq::MC_METROPOLIS) {
+                // rows 0 (accepted) and 1 (probabilities) of the partials; the third row is unused
+                LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->finalize(st, 3, n, 0));
+                const int rc = fetch_out(st, 2);
+                if (rc) return rc;
+                acc += st.h_out[0];
+                psum += st.h_out[1];
+            }
+        }
+    LQ_CK(sync_stream(st));
+    const double n_links = (double)st.V * st.dim;
+    if (n_accepted) *n_accepted = (long long)acc;
+    if (prob_mean) *prob_mean = psum / n_links;
+    return LQ_OK;
+}
+} // namespace
+
+int lq_metropolis_sweep(lq_state *s, int n_update, double spread, uint64_t seed, uint64_t sweep,
+                        long long *n_accepted, double *prob_mean) {
+    LQ_CHECK_STATE(s);
+    // MetropolisHastingsSweep::new (metropolis_hastings_sweep.rs:86-97)
+    if (n_update <= 0 || !(spread > 0.0) || !(spread < 1.0)) return LQ_ERR_INVALID_ARGUMENT;
+    return mc_sweep(s, lq::MC_METROPOLIS, n_update, spread, seed, sweep, n_accepted, prob_mean);
+}
+
+int lq_heat_bath_sweep(lq_state *s, uint64_t seed, uint64_t sweep) {
+    LQ_CHECK_STATE(s);
+    if (!(s->beta > 0.0) || std::isinf(s->beta)) return LQ_ERR_INVALID_ARGUMENT;
+    return mc_sweep(s, lq::MC_HEAT_BATH, 1, 0.5, seed, sweep, nullptr, nullptr);
+}
 
 // ------------------------------------------------------------------ differentiation
 int lq_wilson_action(lq_state *s, double *out) { return lq_hamiltonian_links(s, out); }

@@ -118,6 +118,9 @@ struct Ops {
     cudaError_t (*cot_efield_to_aos)(State &s, const void *lamE, double *d_aos);
     // clover field strength F_ij (i < j) and magnetic field per site, double, serde 3x3 layout
     cudaError_t (*clover_fields)(State &s, const void *U, double *f_out, double *b_out);
+    // one checkerboard class of a Metropolis (0) / heat-bath (1) sweep, in place
+    cudaError_t (*mc_sweep)(State &s, void *U, int alg, int mu, int parity, double beta, uint64_t seed,
+                            uint64_t sweep, int n_update, double spread, uint32_t *n_partials);
 };
 
 const Ops *ops_f64(int dim);

@@ -1,0 +1,335 @@
+// sweeps.cuh -- the reference's local Monte Carlo methods on the device: MetropolisHastingsSweep
+// and HeatBathSweep (src/simulation/monte_carlo/metropolis_hastings_sweep.rs, heat_bath.rs).
+//
+// The reference updates the links one after another in lattice order.  Here a sweep runs in
+// checkerboard order: for each direction mu, every link (x, mu) with sum_i x_i even, then every one
+// with it odd.  The staple of (x, mu) contains U_mu(x +- nu) (the other class) and links of other
+// directions only, so a class updates at once; L must be even for the classes to alternate across
+// the periodic boundary.  Per link the update is the reference's, in double for every storage form
+// (the stored value is split back into hi + lo), with random numbers from a Philox4x32-10 stream per
+// link: counter blocks (link, sweep lo, sweep hi, 0x80000000 + call), two 53-bit uniforms per block.
+// Every rejection loop is bounded (kMaxRedraws draws; the reference loops without a bound).
+#pragma once
+#include "kernels.cuh"
+
+namespace lq {
+
+constexpr int kMaxRedraws = 10000;
+
+// f64::is_normal: finite, not zero, not subnormal (NaN fails both comparisons)
+__device__ __forceinline__ bool is_normal_d(double x) {
+    const double a = fabs(x);
+    return a >= 2.2250738585072014e-308 && a <= 1.7976931348623157e308;
+}
+
+struct LinkRng {
+    uint2 key;
+    uint32_t link, s_lo, s_hi, call;
+    double buf;
+    bool has;
+    __device__ double next() {
+        if (has) {
+            has = false;
+            return buf;
+        }
+        const uint4 r = philox4x32_10(make_uint4(link, s_lo, s_hi, 0x80000000u + call++), key);
+        buf = u01_53(r.z, r.w);
+        has = true;
+        return u01_53(r.x, r.y);
+    }
+    // Uniform::new(a, b): a + (b - a) u, without contraction
+    __device__ double uniform(double a, double b) { return __dadd_rn(a, __dmul_rn(b - a, next())); }
+    __device__ double open_closed01() { return 1.0 - next(); }
+    __device__ bool half() { return next() < 0.5; }
+};
+
+struct m2d {
+    cpx<double> e[4]; // row-major 2x2
+};
+__device__ __forceinline__ cpx<double> cmul(cpx<double> a, cpx<double> b) {
+    return cmk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__device__ __forceinline__ cpx<double> cadd(cpx<double> a, cpx<double> b) { return cmk(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ m2d mul2(const m2d &a, const m2d &b) {
+    m2d r;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) r.e[i * 2 + j] = cadd(cmul(a.e[i * 2], b.e[j]), cmul(a.e[i * 2 + 1], b.e[2 + j]));
+    return r;
+}
+
+// su2::complex_matrix_from_vec (src/su2.rs:134-140): x0 1 + sum_i PAULI_MATRICES[i] (i x_i), with the
+// reference's constants, in which PAULI_3 is the identity (src/su2.rs:13-49):
+//   [[x0 + i x3, x2 + i x1], [-x2 + i x1, x0 + i x3]]
+__device__ __forceinline__ m2d complex_matrix_from_vec(double x0, const double *x) {
+    m2d r;
+    r.e[0] = cmk(x0, x[2]);
+    r.e[1] = cmk(x[1], x[0]);
+    r.e[2] = cmk(-x[1], x[0]);
+    r.e[3] = cmk(x0, x[2]);
+    return r;
+}
+// su2::random_su2_close_to_unity (src/su2.rs:80-100)
+__device__ __forceinline__ m2d random_su2_close_to_unity(double spread, LinkRng &rng) {
+    double r[3], x[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = rng.uniform(-1.0, 1.0);
+    const double n = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) x[i] = (n > 2.220446049250313e-16 ? r[i] / n : r[i]) * spread;
+    const double x0u = sqrt(1.0 - (x[0] * x[0] + x[1] * x[1] + x[2] * x[2]));
+    const double x0 = rng.half() ? x0u : -x0u;
+    return complex_matrix_from_vec(x0, x);
+}
+// su2::random_su2 (src/su2.rs:200-216)
+__device__ __forceinline__ m2d random_su2(LinkRng &rng) {
+    cpx<double> v[2];
+    double n = 0.0;
+    for (int tries = 0; tries < kMaxRedraws; ++tries) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const double re = rng.uniform(-1.0, 1.0);
+            v[k] = cmk(re, rng.uniform(-1.0, 1.0));
+        }
+        n = sqrt(v[0].re * v[0].re + v[0].im * v[0].im + (v[1].re * v[1].re + v[1].im * v[1].im));
+        if (is_normal_d(n)) break;
+    }
+    const cpx<double> a = cmk(v[0].re / n, v[0].im / n), b = cmk(v[1].re / n, v[1].im / n);
+    m2d r;
+    r.e[0] = a;
+    r.e[1] = b;
+    r.e[2] = cmk(-b.re, b.im);
+    r.e[3] = cmk(a.re, -a.im);
+    return r;
+}
+// SU(2) block embedded at rows / columns (p, q) of the identity (su3::get_r, get_s, get_t)
+__device__ __forceinline__ void embed(const m2d &m, int p, int q, mat3<double> &r) {
+    mat_identity(r);
+    r.e[p * 3 + p] = m.e[0];
+    r.e[p * 3 + q] = m.e[1];
+    r.e[q * 3 + p] = m.e[2];
+    r.e[q * 3 + q] = m.e[3];
+}
+// su2::project_to_su2_unorm of the (p, q) sub-block: b - b^dag + 1 conj(Tr b)
+__device__ __forceinline__ m2d su2_unorm(const mat3<double> &in, int p, int q) {
+    m2d b;
+    b.e[0] = in.e[p * 3 + p];
+    b.e[1] = in.e[p * 3 + q];
+    b.e[2] = in.e[q * 3 + p];
+    b.e[3] = in.e[q * 3 + q];
+    const cpx<double> tr = cmk(b.e[0].re + b.e[3].re, -(b.e[0].im + b.e[3].im));
+    m2d r;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const cpx<double> x = b.e[i * 2 + j], y = b.e[j * 2 + i];
+            cpx<double> d = cmk(x.re - y.re, x.im + y.im);
+            if (i == j) d = cadd(d, tr);
+            r.e[i * 2 + j] = d;
+        }
+    return r;
+}
+// su3::random_su3_close_to_unity (src/su3.rs:385-398)
+__device__ __forceinline__ void random_su3_close_to_unity(double spread, LinkRng &rng, mat3<double> &x) {
+    mat3<double> r, s, t, rs;
+    embed(random_su2_close_to_unity(spread, rng), 0, 1, r);
+    embed(random_su2_close_to_unity(spread, rng), 0, 2, s);
+    embed(random_su2_close_to_unity(spread, rng), 1, 2, t);
+    mul_nn(r, s, rs);
+    mul_nn(rs, t, x);
+    if (rng.half()) {
+        mat3<double> a = x;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) x.e[i * 3 + j] = cmk(a.e[j * 3 + i].re, -a.e[j * 3 + i].im);
+    }
+}
+// statistics::ModifiedNormal, HeatBathDistributionNorm, HeatBathDistribution
+// (src/statistics/distribution.rs:76-101, :320-350, :199-218)
+__device__ __forceinline__ double modified_normal(double param, LinkRng &rng) {
+    double r[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = rng.open_closed01();
+    const double c = cos(2.0 * 3.141592653589793 * r[1]);
+    return sqrt(-(log(r[0]) + c * c * log(r[2])) / (2.0 * param));
+}
+__device__ __forceinline__ m2d heat_bath_sample(double param, LinkRng &rng) {
+    double x0 = 1.0;
+    for (int tries = 0; tries < kMaxRedraws; ++tries) {
+        const double r = rng.uniform(0.0, 1.0);
+        const double lambda = modified_normal(param, rng);
+        if (r * r <= 1.0 - lambda * lambda) {
+            x0 = 1.0 - 2.0 * lambda * lambda;
+            break;
+        }
+    }
+    double x[3], n = 0.0;
+    for (int tries = 0; tries < kMaxRedraws; ++tries) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) x[i] = rng.uniform(-1.0, 1.0);
+        n = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        if (n > 2.220446049250313e-16) break;
+    }
+    const double f = sqrt(1.0 - x0 * x0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) x[i] = x[i] / n * f;
+    return complex_matrix_from_vec(x0, x);
+}
+// HeatBathSweep::heat_bath_su2 (heat_bath.rs:71-86)
+__device__ __forceinline__ m2d heat_bath_su2(const m2d &st, double beta, LinkRng &rng) {
+    const cpx<double> det = cmk(st.e[0].re * st.e[3].re - st.e[0].im * st.e[3].im -
+                                    (st.e[2].re * st.e[1].re - st.e[2].im * st.e[1].im),
+                                0.0);
+    const double k = sqrt(det.re);
+    if (is_normal_d(k)) {
+        m2d v;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const cpx<double> z = st.e[j * 2 + i]; // adjoint
+                v.e[i * 2 + j] = cmk(z.re * k / (k * k), -z.im * k / (k * k));
+            }
+        return mul2(heat_bath_sample(beta * k, rng), v);
+    }
+    return random_su2(rng);
+}
+
+// the link (site, mu) and its neighbours as double (hi + lo with compensated storage)
+template <typename T, bool COMP>
+__device__ __forceinline__ void load_link_d(const V2<T> *__restrict__ U, size_t ulo, size_t i, mat3<double> &m) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const V2<T> h = U[i + k * kTile];
+        double re = (double)h.x, im = (double)h.y;
+        if (COMP) {
+            const V2<T> l = U[ulo + i + k * kTile];
+            re += (double)l.x;
+            im += (double)l.y;
+        }
+        m.e[k] = cmk(re, im);
+    }
+}
+template <typename T, bool COMP>
+__device__ __forceinline__ void store_link_d(V2<T> *__restrict__ U, size_t ulo, size_t i, const mat3<double> &m) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        V2<T> h, l;
+        split(m.e[k].re, h.x, l.x);
+        split(m.e[k].im, h.y, l.y);
+        U[i + k * kTile] = h;
+        if (COMP) U[ulo + i + k * kTile] = l;
+    }
+}
+// the staple of the Monte Carlo methods (src/simulation/monte_carlo/mod.rs:339-362):
+// sum over nu != mu of S_mu,nu(x)^dag + U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)
+template <int D, typename T, bool COMP>
+__device__ __forceinline__ void mc_staple(const V2<T> *__restrict__ U, size_t ulo, const Geo<D> &g, uint32_t site,
+                                          const uint32_t *c, int mu, mat3<double> &sum) {
+    const uint32_t xpmu = fwd(g, site, c[mu], mu);
+    mat_zero(sum);
+#pragma unroll 1
+    for (int nu = 0; nu < D; ++nu) {
+        if (nu == mu) continue;
+        mat3<double> a, b, t, term;
+        // S^dag = U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag
+        load_link_d<T, COMP>(U, ulo, tix(xpmu, D * 9, nu * 9), a);
+        load_link_d<T, COMP>(U, ulo, tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), b);
+        mul_na(a, b, t);
+        load_link_d<T, COMP>(U, ulo, tix(site, D * 9, nu * 9), a);
+        mul_na(t, a, term);
+        // U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu) = (U_mu(x-nu) U_nu(x+mu-nu))^dag U_nu(x-nu)
+        const uint32_t xmnu = bwd(g, site, c[nu], nu);
+        load_link_d<T, COMP>(U, ulo, tix(bwd(g, xpmu, c[nu], nu), D * 9, nu * 9), a);
+        load_link_d<T, COMP>(U, ulo, tix(xmnu, D * 9, mu * 9), b);
+        mat3<double> ba;
+        mul_nn(b, a, ba);
+        load_link_d<T, COMP>(U, ulo, tix(xmnu, D * 9, nu * 9), a);
+        mul_an(ba, a, t);
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            sum.e[k] = cmk(sum.e[k].re + (term.e[k].re + t.e[k].re), sum.e[k].im + (term.e[k].im + t.e[k].im));
+    }
+}
+
+enum : int { MC_METROPOLIS = 0, MC_HEAT_BATH = 1 };
+
+// One checkerboard class of a sweep: links (x, mu) with parity(x) = parity.  Metropolis partials:
+// row 0 accepted count, row 1 sum of acceptance probabilities (per block).
+template <int D, typename T, bool COMP, int ALG>
+__global__ void __launch_bounds__(128) k_mc_sweep(V2<T> *__restrict__ U, Geo<D> g, int mu, int parity, double beta,
+                                                  uint2 key, uint32_t s_lo, uint32_t s_hi, int n_update,
+                                                  double spread, double *__restrict__ partial) {
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    uint32_t c[D];
+    bool active = site < g.V;
+    if (active) {
+        site_coords(g, site, c);
+        uint32_t p = 0;
+#pragma unroll
+        for (int i = 0; i < D; ++i) p += c[i];
+        active = (int)(p & 1u) == parity;
+    }
+    if (active) {
+        const size_t ulo = (size_t)tiles_of(g.V) * D * 9 * kTile;
+        const size_t ui = tix(site, D * 9, mu * 9);
+        LinkRng rng{key, site * D + (uint32_t)mu, s_lo, s_hi, 0u, 0.0, false};
+        mat3<double> u, a, out;
+        load_link_d<T, COMP>(U, ulo, ui, u);
+        if (ALG == MC_METROPOLIS) {
+            // MetropolisHastingsSweep::potential_modif and the accept test (metropolis_hastings_sweep.rs:120-172)
+            mat3<double> nm = u, r, t;
+            for (int k = 0; k < n_update; ++k) {
+                random_su3_close_to_unity(spread, rng, r);
+                double re[9], im[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    re[q] = r.e[q].re;
+                    im[q] = r.e[q].im;
+                }
+                orthonormalize_d(re, im);
+#pragma unroll
+                for (int q = 0; q < 9; ++q) r.e[q] = cmk(re[q], im[q]);
+                mul_nn(r, nm, t);
+                nm = t;
+            }
+            mc_staple<D, T, COMP>(U, ulo, g, site, c, mu, a);
+            // delta_s_old_new_cmp (mod.rs:324-334): -Re Tr((U' - U) A) beta / 3
+            mat3<double> d;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) d.e[q] = cmk(nm.e[q].re - u.e[q].re, nm.e[q].im - u.e[q].im);
+            mul_nn(d, a, t);
+            const double ds = -(t.e[0].re + t.e[4].re + t.e[8].re) * beta / 3.0;
+            const double p = fmax(fmin(exp(-ds), 1.0), 0.0);
+            v[1] = p;
+            if (p >= 1.0 || rng.next() < p) {
+                store_link_d<T, COMP>(U, ulo, ui, nm);
+                v[0] = 1.0;
+            }
+        } else {
+            // HeatBathSweep::get_modif (heat_bath.rs:88-108): U' = t s r U
+            mc_staple<D, T, COMP>(U, ulo, g, site, c, mu, a);
+            mat3<double> ua, r, s, t, x, y;
+            mul_nn(u, a, ua);
+            embed(heat_bath_su2(su2_unorm(ua, 0, 1), beta, rng), 0, 1, r);
+            mul_nn(r, u, x);
+            mul_nn(x, a, y);
+            embed(heat_bath_su2(su2_unorm(y, 0, 2), beta, rng), 0, 2, s);
+            mul_nn(s, r, x);
+            mul_nn(x, u, y);
+            mul_nn(y, a, x);
+            embed(heat_bath_su2(su2_unorm(x, 1, 2), beta, rng), 1, 2, t);
+            mul_nn(t, s, x);
+            mul_nn(x, r, y);
+            mul_nn(y, u, out);
+            store_link_d<T, COMP>(U, ulo, ui, out);
+        }
+    }
+    if (ALG == MC_METROPOLIS) block_reduce_store<2>(v, partial, blockIdx.x, gridDim.x);
+}
+
+} // namespace lq

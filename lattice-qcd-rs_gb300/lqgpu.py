@@ -78,6 +78,8 @@ SIGNATURES = {
     "lq_wilson_action": (_i32, [_vp, _dp]),
     "lq_wilson_action_backward": (_i32, [_vp, _dp, _sz]),
     "lq_link_rotate": (_i32, [_vp, ctypes.c_longlong, _i32, _f64]),
+    "lq_metropolis_sweep": (_i32, [_vp, _i32, _f64, _u64, _u64, _llp, _dp]),
+    "lq_heat_bath_sweep": (_i32, [_vp, _u64, _u64]),
     "lq_field_strength": (_i32, [_vp, _dp, _sz]),
     "lq_magnetic_field": (_i32, [_vp, _dp, _sz]),
     "lq_leapfrog_adjoint": (_i32, [_vp, _f64, _i32, _i32, _dp, _dp, _dp, _sz, _dp, _sz, _szp]),
@@ -287,6 +289,17 @@ class State:
         _check(load().lq_link_rotate(self._h, link, generator, angle), "lq_link_rotate")
 
     # ---- updates
+    def metropolis_sweep(self, n_update, spread, seed, sweep):
+        """one checkerboard MetropolisHastingsSweep; returns (accepted updates, mean probability)"""
+        acc, pm = ctypes.c_longlong(), ctypes.c_double()
+        _check(load().lq_metropolis_sweep(self._h, n_update, spread, seed, sweep, ctypes.byref(acc),
+                                          ctypes.byref(pm)), "lq_metropolis_sweep")
+        return acc.value, pm.value
+
+    def heat_bath_sweep(self, seed, sweep):
+        """one checkerboard HeatBathSweep"""
+        _check(load().lq_heat_bath_sweep(self._h, seed, sweep), "lq_heat_bath_sweep")
+
     def field_strength(self):
         """F_ij (clover) at every site for the planes i < j: float64[V, D(D-1)/2, 18]"""
         out = np.empty((self.L ** self.dim, self.dim * (self.dim - 1) // 2, 18))

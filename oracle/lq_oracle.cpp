@@ -710,6 +710,221 @@ Fields integrate_once(const Lattice &lat, const Fields &in, double size, int mod
     return out;
 }
 
+/* ---- Monte Carlo sweeps: MetropolisHastingsSweep and HeatBathSweep
+ * (src/simulation/monte_carlo/metropolis_hastings_sweep.rs, heat_bath.rs), per link as the reference
+ * updates it, in checkerboard order (for each direction mu, all links (x, mu) with sum_i x_i even,
+ * then odd: links of one class share no staple, so the class can be updated at once) with random
+ * numbers from a Philox4x32-10 stream per link (the device's stream; the reference's rand streams
+ * are not restated). */
+
+/* Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11) */
+struct U4 {
+    uint32_t x, y, z, w;
+};
+inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+        c = U4{(uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0};
+    }
+    return c;
+}
+/* uniforms in [0, 1) with 53 bits from counter blocks (link, sweep lo, sweep hi, 0x80000000 + call) */
+struct LinkRng {
+    uint32_t k0, k1, link, s_lo, s_hi;
+    uint32_t call = 0;
+    double buf = 0.0;
+    bool has = false;
+    static double u01(uint32_t hi, uint32_t lo) {
+        return (double)((((uint64_t)hi << 32) | lo) >> 11) * (1.0 / 9007199254740992.0);
+    }
+    double next() {
+        if (has) {
+            has = false;
+            return buf;
+        }
+        const U4 r = philox4x32_10(U4{link, s_lo, s_hi, 0x80000000u + call++}, k0, k1);
+        buf = u01(r.z, r.w);
+        has = true;
+        return u01(r.x, r.y);
+    }
+    double uniform(double a, double b) { return a + (b - a) * next(); } /* Uniform::new(a, b) */
+    double open_closed01() { return 1.0 - next(); }                    /* OpenClosed01 */
+    bool half() { return next() < 0.5; }                               /* Bernoulli(0.5) */
+};
+
+constexpr int kMaxRedraws = 10000; /* bound of every rejection loop (the reference loops without one) */
+
+struct M2 {
+    Cx m[2][2];
+};
+inline M2 mul2(const M2 &a, const M2 &b) {
+    M2 r;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) r.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j];
+    return r;
+}
+inline M2 adj2(const M2 &a) {
+    M2 r;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) r.m[i][j] = conj(a.m[j][i]);
+    return r;
+}
+/* su2::complex_matrix_from_vec (src/su2.rs:134-140): x0 1 + sum_i PAULI_MATRICES[i] (i x_i), with the
+ * reference's constants PAULI_1 = [[0,1],[1,0]], PAULI_2 = [[0,-i],[i,0]], PAULI_3 = [[1,0],[0,1]]
+ * (src/su2.rs:13-49: PAULI_3 is written as the identity) */
+inline M2 complex_matrix_from_vec(double x0, const double *x) {
+    static const Cx P[3][2][2] = {{{{0, 0}, {1, 0}}, {{1, 0}, {0, 0}}},
+                                  {{{0, 0}, {0, -1}}, {{0, 1}, {0, 0}}},
+                                  {{{1, 0}, {0, 0}}, {{0, 0}, {1, 0}}}};
+    M2 r;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+            Cx t = cx(0.0, 0.0);
+            for (int k = 0; k < 3; ++k) t = t + P[k][i][j] * Cx{0.0, x[k]};
+            r.m[i][j] = Cx{i == j ? 1.0 : 0.0, 0.0} * Cx{x0, 0.0} + t;
+        }
+    return r;
+}
+/* su2::random_su2_close_to_unity (src/su2.rs:80-100) */
+inline M2 random_su2_close_to_unity(double spread, LinkRng &rng) {
+    double r[3];
+    for (double &v : r) v = rng.uniform(-1.0, 1.0);
+    const double n = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    double x[3];
+    for (int i = 0; i < 3; ++i) x[i] = (n > F64_EPS ? r[i] / n : r[i]) * spread;
+    const double x0u = std::sqrt(1.0 - (x[0] * x[0] + x[1] * x[1] + x[2] * x[2]));
+    const double x0 = rng.half() ? x0u : -x0u;
+    return complex_matrix_from_vec(x0, x);
+}
+/* su2::random_su2 (src/su2.rs:200-216) */
+inline M2 random_su2(LinkRng &rng) {
+    Cx v[2];
+    double n = 0.0;
+    for (int tries = 0; tries < kMaxRedraws; ++tries) {
+        for (Cx &c : v) {
+            const double re = rng.uniform(-1.0, 1.0);
+            c = Cx{re, rng.uniform(-1.0, 1.0)};
+        }
+        n = std::sqrt(modulus_squared(v[0]) + modulus_squared(v[1]));
+        if (std::isnormal(n)) break;
+    }
+    const Cx d{n, 0.0};
+    auto divc = [&](Cx a) { /* num-complex division by (n, 0) */
+        const double q = d.re * d.re + d.im * d.im;
+        return Cx{(a.re * d.re + a.im * d.im) / q, (a.im * d.re - a.re * d.im) / q};
+    };
+    const Cx a = divc(v[0]), b = divc(v[1]);
+    M2 r;
+    r.m[0][0] = a;
+    r.m[0][1] = b;
+    r.m[1][0] = Cx{-b.re, b.im}; /* -conj(b) */
+    r.m[1][1] = conj(a);
+    return r;
+}
+/* su3::get_r / get_s / get_t (src/su3.rs:428-530): SU(2) blocks embedded at (0,1), (0,2), (1,2) */
+inline M3 embed(const M2 &m, int p, int q) {
+    M3 r = identity3();
+    r.m[p][p] = m.m[0][0];
+    r.m[p][q] = m.m[0][1];
+    r.m[q][p] = m.m[1][0];
+    r.m[q][q] = m.m[1][1];
+    return r;
+}
+/* su3::get_su2_*_unorm (src/su3.rs:559-659): su2::project_to_su2_unorm(m) = m - m^dag + 1 conj(Tr m)
+ * of the sub-block */
+inline M2 su2_unorm(const M3 &in, int p, int q) {
+    M2 b;
+    b.m[0][0] = in.m[p][p];
+    b.m[0][1] = in.m[p][q];
+    b.m[1][0] = in.m[q][p];
+    b.m[1][1] = in.m[q][q];
+    const Cx tr = conj(b.m[0][0] + b.m[1][1]);
+    M2 r;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) r.m[i][j] = (b.m[i][j] - conj(b.m[j][i])) + Cx{i == j ? 1.0 : 0.0, 0.0} * tr;
+    return r;
+}
+/* su3::random_su3_close_to_unity (src/su3.rs:385-398) */
+inline M3 random_su3_close_to_unity(double spread, LinkRng &rng) {
+    const M3 r = embed(random_su2_close_to_unity(spread, rng), 0, 1);
+    const M3 s = embed(random_su2_close_to_unity(spread, rng), 0, 2);
+    const M3 t = embed(random_su2_close_to_unity(spread, rng), 1, 2);
+    M3 x = (r * s) * t;
+    if (rng.half()) x = adjoint(x);
+    return x;
+}
+/* statistics::ModifiedNormal, HeatBathDistributionNorm, HeatBathDistribution
+ * (src/statistics/distribution.rs:76-101, :320-350, :199-218) */
+inline double modified_normal(double param, LinkRng &rng) {
+    double r[3];
+    for (double &v : r) v = rng.open_closed01();
+    const double c = std::cos(2.0 * 3.141592653589793 * r[1]);
+    return std::sqrt(-(std::log(r[0]) + c * c * std::log(r[2])) / (2.0 * param));
+}
+inline double heat_bath_norm(double param, LinkRng &rng) {
+    for (int tries = 0; tries < kMaxRedraws; ++tries) {
+        const double r = rng.uniform(0.0, 1.0);
+        const double lambda = modified_normal(param, rng);
+        if (r * r <= 1.0 - lambda * lambda) return 1.0 - 2.0 * lambda * lambda;
+    }
+    return 1.0;
+}
+inline M2 heat_bath_sample(double param, LinkRng &rng) {
+    const double x0 = heat_bath_norm(param, rng);
+    double x[3], n = 0.0;
+    for (int tries = 0; tries < kMaxRedraws; ++tries) {
+        for (double &v : x) v = rng.uniform(-1.0, 1.0);
+        n = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        if (n > F64_EPS) break;
+    }
+    const double f = std::sqrt(1.0 - x0 * x0);
+    for (double &v : x) v = v / n * f;
+    return complex_matrix_from_vec(x0, x);
+}
+/* HeatBathSweep::heat_bath_su2 (src/simulation/monte_carlo/heat_bath.rs:71-86) */
+inline M2 heat_bath_su2(const M2 &staple, double beta, LinkRng &rng) {
+    const Cx det = staple.m[0][0] * staple.m[1][1] - staple.m[1][0] * staple.m[0][1];
+    const double k = std::sqrt(det.re);
+    if (std::isnormal(k)) {
+        const M2 a = adj2(staple);
+        M2 v;
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j) {
+                const Cx z = a.m[i][j];
+                const double q = k * k;
+                v.m[i][j] = Cx{(z.re * k) / q, (z.im * k) / q};
+            }
+        return mul2(heat_bath_sample(beta * k, rng), v);
+    }
+    return random_su2(rng);
+}
+/* the staple of the Monte Carlo methods (src/simulation/monte_carlo/mod.rs:339-362):
+ * sum over nu != mu of S_mu,nu(x)^dag + U_{-nu}(x+mu) U_mu(x-nu)^dag U_nu(x-nu) */
+inline M3 mc_staple(const Lattice &lat, const double *links, long site, int mu) {
+    M3 sum = zero3();
+    for (int nu = 0; nu < lat.D; ++nu) {
+        if (nu == mu) continue;
+        const M3 el1 = adjoint(sij(lat, links, site, Dir{mu, true}, Dir{nu, true}));
+        const long xpmu = lat.neighbour(site, mu, true);
+        const M3 u1 = link_matrix(lat, links, xpmu, Dir{nu, false});
+        const long xmnu = lat.neighbour(site, nu, false);
+        const M3 u2 = adjoint(link_matrix(lat, links, xmnu, Dir{mu, true}));
+        const M3 u3 = link_matrix(lat, links, xmnu, Dir{nu, true});
+        sum = sum + (el1 + (u1 * u2) * u3);
+    }
+    return sum;
+}
+inline long parity_of(const Lattice &lat, long site) {
+    long x[4], p = 0;
+    lat.coords(site, x);
+    for (int i = 0; i < lat.D; ++i) p += x[i];
+    return p & 1;
+}
+
 bool supported_dim(int dim) { return dim >= 2 && dim <= 4; }
 
 int check_lattice(int dim, long L) {
@@ -845,6 +1060,65 @@ int or_magnetic_field(int dim, int L, double size, const double *links, long sit
     const Lattice lat(dim, L);
     if (site < 0 || site >= lat.V || k < 0 || k >= dim) return OR_ERR_INVALID_ARGUMENT;
     store_m3(magnetic_field(lat, size, links, site, k), out18);
+    return OR_OK;
+}
+/* MetropolisHastingsSweep::next_element (metropolis_hastings_sweep.rs:147-177) in checkerboard
+ * order; link (site, mu) draws from LinkRng(seed, link = site * D + mu, sweep) */
+int or_metropolis_sweep(int dim, int L, double beta, const double *links_in, int n_update, double spread,
+                        uint64_t seed, uint64_t sweep, double *links_out, long *n_accepted, double *prob_sum) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    if (L % 2 != 0 || n_update <= 0 || !(spread > 0.0) || !(spread < 1.0)) return OR_ERR_INVALID_ARGUMENT;
+    const Lattice lat(dim, L);
+    std::memcpy(links_out, links_in, sizeof(double) * 18 * lat.V * dim);
+    long acc = 0;
+    double psum = 0.0;
+    for (int mu = 0; mu < dim; ++mu)
+        for (long parity = 0; parity < 2; ++parity)
+            for (long site = 0; site < lat.V; ++site) {
+                if (parity_of(lat, site) != parity) continue;
+                LinkRng rng{(uint32_t)seed, (uint32_t)(seed >> 32), (uint32_t)(site * dim + mu), (uint32_t)sweep,
+                            (uint32_t)(sweep >> 32)};
+                double *lp = links_out + (site * dim + mu) * 18;
+                const M3 old_m = load_m3(lp);
+                M3 new_m = old_m;
+                for (int k = 0; k < n_update; ++k)
+                    new_m = orthonormalize_matrix(random_su3_close_to_unity(spread, rng)) * new_m;
+                const M3 a = mc_staple(lat, links_out, site, mu);
+                const double ds = -trace((new_m - old_m) * a).re * beta / 3.0;
+                const double p = std::fmax(std::fmin(std::exp(-ds), 1.0), 0.0);
+                psum += p;
+                if (p >= 1.0 || rng.next() < p) {
+                    store_m3(new_m, lp);
+                    ++acc;
+                }
+            }
+    if (n_accepted) *n_accepted = acc;
+    if (prob_sum) *prob_sum = psum;
+    return OR_OK;
+}
+/* HeatBathSweep::next_element (heat_bath.rs:88-121) in checkerboard order */
+int or_heat_bath_sweep(int dim, int L, double beta, const double *links_in, uint64_t seed, uint64_t sweep,
+                       double *links_out) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    if (L % 2 != 0 || !(beta > 0.0)) return OR_ERR_INVALID_ARGUMENT;
+    const Lattice lat(dim, L);
+    std::memcpy(links_out, links_in, sizeof(double) * 18 * lat.V * dim);
+    for (int mu = 0; mu < dim; ++mu)
+        for (long parity = 0; parity < 2; ++parity)
+            for (long site = 0; site < lat.V; ++site) {
+                if (parity_of(lat, site) != parity) continue;
+                LinkRng rng{(uint32_t)seed, (uint32_t)(seed >> 32), (uint32_t)(site * dim + mu), (uint32_t)sweep,
+                            (uint32_t)(sweep >> 32)};
+                double *lp = links_out + (site * dim + mu) * 18;
+                const M3 u = load_m3(lp);
+                const M3 a = mc_staple(lat, links_out, site, mu);
+                const M3 r = embed(heat_bath_su2(su2_unorm(u * a, 0, 1), beta, rng), 0, 1);
+                const M3 s = embed(heat_bath_su2(su2_unorm((r * u) * a, 0, 2), beta, rng), 0, 2);
+                const M3 t = embed(heat_bath_su2(su2_unorm(((s * r) * u) * a, 1, 2), beta, rng), 1, 2);
+                store_m3(((t * s) * r) * u, lp);
+            }
     return OR_OK;
 }
 int or_gauss(int dim, int L, const double *links, const double *efield, long site, double *out18) {

@@ -80,6 +80,11 @@ int or_average_trace_plaquette(int dim, int L, const double *links, double *re, 
 int or_clover(int dim, int L, const double *links, long site, int i, int i_pos, int j, int j_pos, double *out18);
 int or_f_mu_nu(int dim, int L, double size, const double *links, long site, int i, int j, double *out18);
 int or_magnetic_field(int dim, int L, double size, const double *links, long site, int k, double *out18);
+/* MetropolisHastingsSweep / HeatBathSweep in checkerboard order, Philox stream per link (see the source) */
+int or_metropolis_sweep(int dim, int L, double beta, const double *links_in, int n_update, double spread,
+                        uint64_t seed, uint64_t sweep, double *links_out, long *n_accepted, double *prob_sum);
+int or_heat_bath_sweep(int dim, int L, double beta, const double *links_in, uint64_t seed, uint64_t sweep,
+                       double *links_out);
 int or_gauss(int dim, int L, const double *links, const double *efield, long site, double *out18);
 int or_gauss_sum_div(int dim, int L, const double *links, const double *efield, double *out);
 int or_project_to_gauss(int dim, int L, const double *links, const double *efield_in,

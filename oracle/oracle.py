@@ -68,6 +68,9 @@ def lib():
             "or_average_trace_plaquette": (i32, [i32, i32, _dp, _dp, _dp]),
             "or_gauss": (i32, [i32, i32, _dp, _dp, lng, _dp]),
             "or_clover": (i32, [i32, i32, _dp, lng, i32, i32, i32, i32, _dp]),
+            "or_metropolis_sweep": (i32, [i32, i32, ctypes.c_double, _dp, i32, ctypes.c_double, u64, u64, _dp,
+                                          ctypes.POINTER(ctypes.c_long), _dp]),
+            "or_heat_bath_sweep": (i32, [i32, i32, ctypes.c_double, _dp, u64, u64, _dp]),
             "or_f_mu_nu": (i32, [i32, i32, ctypes.c_double, _dp, lng, i32, i32, _dp]),
             "or_magnetic_field": (i32, [i32, i32, ctypes.c_double, _dp, lng, i32, _dp]),
             "or_gauss_sum_div": (i32, [i32, i32, _dp, _dp, _dp]),
@@ -226,6 +229,24 @@ def average_trace_plaquette(dim, L, links):
 def gauss(dim, L, links, efield, site):
     out = np.zeros(18)
     _check(lib().or_gauss(dim, L, _p(links), _p(efield), site, _p(out)), "gauss")
+    return out
+
+
+def metropolis_sweep(dim, L, beta, links, n_update, spread, seed, sweep):
+    """checkerboard MetropolisHastingsSweep with the per-link Philox stream; (links, accepted, sum p)"""
+    out = np.zeros_like(links)
+    acc = ctypes.c_long(0)
+    ps = np.zeros(1)
+    _check(lib().or_metropolis_sweep(dim, L, beta, _p(np.ascontiguousarray(links)), n_update, spread, seed, sweep,
+                                     _p(out), ctypes.byref(acc), _p(ps)), "metropolis_sweep")
+    return out, acc.value, float(ps[0])
+
+
+def heat_bath_sweep(dim, L, beta, links, seed, sweep):
+    """checkerboard HeatBathSweep with the per-link Philox stream"""
+    out = np.zeros_like(links)
+    _check(lib().or_heat_bath_sweep(dim, L, beta, _p(np.ascontiguousarray(links)), seed, sweep, _p(out)),
+           "heat_bath_sweep")
     return out
 
 

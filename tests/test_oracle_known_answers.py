@@ -284,3 +284,31 @@ def test_clover_and_magnetic_field_known_answers(oracle_mod):
     # the point [4, 0, 0] wraps to [0, 0, 0]
     b = O.magnetic_field(dim, L, size, links, 0, 2)
     assert np.array_equal(b, O.magnetic_field(dim, L, size, links, 4 % L, 2))
+
+
+def test_checkerboard_sweeps_restatement(oracle_mod):
+    """Properties of the oracle's checkerboard MetropolisHastingsSweep / HeatBathSweep: the same
+    (seed, sweep) gives the same links, another sweep counter other links; Metropolis keeps links in
+    SU(3) (its proposals are orthonormalised) and reports accepted counts within [0, links]; the
+    argument checks of MetropolisHastingsSweep::new; odd L refused.  The heat bath follows the
+    reference's complex_matrix_from_vec, whose third Pauli constant is the identity
+    (src/su2.rs:40-46), so its links leave SU(3)."""
+    O = oracle_mod
+    dim, L, beta = 4, 4, 2.0
+    links = O.links_random(dim, L, O.Rng(6))
+    a, acc_a, ps_a = O.metropolis_sweep(dim, L, beta, links, 1, 0.1, 3, 0)
+    b, acc_b, ps_b = O.metropolis_sweep(dim, L, beta, links, 1, 0.1, 3, 0)
+    c, _, _ = O.metropolis_sweep(dim, L, beta, links, 1, 0.1, 3, 1)
+    assert np.array_equal(a, b) and acc_a == acc_b and ps_a == ps_b
+    assert not np.array_equal(a, c)
+    n = L ** dim * dim
+    assert 0 < acc_a < n and 0.0 < ps_a / n < 1.0
+    U = np.array([O.to_complex(m) for m in a])
+    assert np.abs(U @ U.conj().transpose(0, 2, 1) - np.eye(3)).max() < 1e-13
+    h = O.heat_bath_sweep(dim, L, beta, links, 3, 0)
+    assert np.isfinite(h).all() and not np.array_equal(h, links)
+    for bad in ((0, 0.1), (1, 0.0), (1, 1.0)):
+        with pytest.raises(Exception):
+            O.metropolis_sweep(dim, L, beta, links, bad[0], bad[1], 3, 0)
+    with pytest.raises(Exception):
+        O.heat_bath_sweep(dim, 3, beta, O.links_cold(dim, 3), 3, 0)

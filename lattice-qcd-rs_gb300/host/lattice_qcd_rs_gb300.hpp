@@ -457,6 +457,59 @@ template <int D> struct WilsonAction {
 // (src/simulation/monte_carlo/hybrid_monte_carlo.rs:302-614).  next_element draws the momenta
 // (device Philox keyed by the generator), projects them, integrates, and accepts with
 // Bernoulli(prob): prob == 1 accepts without drawing, otherwise one uniform u < prob.
+// MetropolisHastingsSweep (src/simulation/monte_carlo/metropolis_hastings_sweep.rs) on the device:
+// one next_element is one checkerboard sweep (lq_metropolis_sweep); the Philox seed of the sweeps is
+// drawn from the Rng once, the sweep counter advances per call.
+template <class Rng = Xoshiro256PlusPlus> class MetropolisHastingsSweep {
+  public:
+    // MetropolisHastingsSweep::new: None unless number_of_update >= 1 and 0 < spread < 1
+    static std::optional<MetropolisHastingsSweep> new_(std::size_t number_of_update, Real spread, Rng rng) {
+        if (number_of_update == 0 || !(spread > 0.0) || !(spread < 1.0)) return std::nullopt;
+        return MetropolisHastingsSweep(number_of_update, spread, std::move(rng));
+    }
+    template <int D> Result<LatticeStateDefault<D>> next_element(LatticeStateDefault<D> state) {
+        long long acc = 0;
+        double pm = 0.0;
+        const int rc = lq_metropolis_sweep(state.raw(), (int)n_, spread_, seed_, sweep_++, &acc, &pm);
+        if (rc) return Result<LatticeStateDefault<D>>::err(rc);
+        state.invalidate_mirror();
+        number_replace_last_ = (std::size_t)acc;
+        prob_replace_mean_ = pm;
+        return Result<LatticeStateDefault<D>>::ok(std::move(state));
+    }
+    std::size_t number_replace_last() const { return number_replace_last_; }
+    Real prob_replace_mean() const { return prob_replace_mean_; }
+
+  private:
+    MetropolisHastingsSweep(std::size_t n, Real spread, Rng rng)
+        : n_(n), spread_(spread), rng_(std::move(rng)), seed_(rng_.next_u64()) {}
+    std::size_t n_;
+    Real spread_;
+    Rng rng_;
+    uint64_t seed_;
+    uint64_t sweep_ = 0;
+    std::size_t number_replace_last_ = 0;
+    Real prob_replace_mean_ = 0.0;
+};
+
+// HeatBathSweep (src/simulation/monte_carlo/heat_bath.rs) on the device: one checkerboard sweep per
+// next_element (lq_heat_bath_sweep)
+template <class Rng = Xoshiro256PlusPlus> class HeatBathSweep {
+  public:
+    explicit HeatBathSweep(Rng rng) : rng_(std::move(rng)), seed_(rng_.next_u64()) {}
+    template <int D> Result<LatticeStateDefault<D>> next_element(LatticeStateDefault<D> state) {
+        const int rc = lq_heat_bath_sweep(state.raw(), seed_, sweep_++);
+        if (rc) return Result<LatticeStateDefault<D>>::err(rc);
+        state.invalidate_mirror();
+        return Result<LatticeStateDefault<D>>::ok(std::move(state));
+    }
+
+  private:
+    Rng rng_;
+    uint64_t seed_;
+    uint64_t sweep_ = 0;
+};
+
 template <int D, class Rng = Xoshiro256PlusPlus, class I = SymplecticEulerGpu> class HybridMonteCarloDiagnostic {
   public:
     HybridMonteCarloDiagnostic(Real delta_t, std::size_t number_of_steps, I integrator, Rng rng)

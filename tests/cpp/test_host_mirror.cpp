@@ -108,6 +108,23 @@ int main() {
         CHECK(worst == 0.0);
     }
 
+    // the local sweeps through monte_carlo_step: Metropolis keeps the plaquette of a cold start
+    // near 3 at beta = 8 and reports accepted updates; the argument checks of ::new
+    {
+        CHECK(!MetropolisHastingsSweep<>::new_(0, 0.1, Xoshiro256PlusPlus::seed_from_u64(1)).has_value());
+        CHECK(!MetropolisHastingsSweep<>::new_(1, 1.0, Xoshiro256PlusPlus::seed_from_u64(1)).has_value());
+        auto mh = MetropolisHastingsSweep<>::new_(1, 0.1, Xoshiro256PlusPlus::seed_from_u64(1)).value();
+        auto st = LatticeStateDefault<4>::new_cold(1.0, 8.0, 4).unwrap();
+        for (int i = 0; i < 3; ++i) st = std::move(st).monte_carlo_step(mh).unwrap();
+        CHECK(mh.number_replace_last() > 0);
+        CHECK(st.average_trace_plaquette().value().real() > 2.5);
+        HeatBathSweep<> hb(Xoshiro256PlusPlus::seed_from_u64(2));
+        st = std::move(st).monte_carlo_step(hb).unwrap();
+        CHECK(std::isfinite(st.average_trace_plaquette().value().real()));
+        auto odd = LatticeStateDefault<4>::new_cold(1.0, 8.0, 3).unwrap();
+        CHECK(hb.next_element(std::move(odd)).error() == LQ_ERR_INVALID_ARGUMENT);
+    }
+
     // setter with a wrong size panics, as the reference's set_link_matrix does
     {
         auto s = LatticeStateDefault<2>::new_cold(1.0, 1.0, 4).unwrap();

@@ -22,7 +22,11 @@ batch     : 64 ensembles of uneven side length and beta advanced together (one l
 adjoint   : d<plaq>/dbeta through a 50-step leap-frog at 48^4 by the checkpointed reverse-mode
             adjoint, FP32 and FP64, each against its central difference in beta.
 
+distribution: HMC and checkerboard Metropolis on the same lattice and beta give the same average
+            plaquette within statistical errors (both sample the Wilson measure).
+
 usage: python studies.py precision [--traj N] | scale [--traj K] | batch [--traj N] | adjoint [--L 48]
+       | distribution [--therm N --meas M]
 """
 import argparse
 import json
@@ -317,14 +321,89 @@ def adjoint_study(args):
     return out
 
 
+def distribution_study(args):
+    """Two samplers of the same Wilson measure exp(-beta sum (1 - Re Tr P / 3)) on the device: HMC
+    with the exponential link update (the reference's molecular dynamics carries no beta; momenta
+    N(0, 0.5/beta) make the links' marginal the Wilson measure) and checkerboard Metropolis.  D = 4, 8^4, beta 2 and 4 (smaller betas
+    give momenta for which the reference's Gauss projection diverges), random start; the average plaquette <Re Tr P>/3 over the measured part of each chain, with its error
+    from blocks of 20 measurements."""
+    dim, L = 4, 8
+    out = {"study": "distribution", "dim": dim, "L": L, "betas": {}}
+
+    def mean_err(x, block=20):
+        x = np.asarray(x)
+        nb = len(x) // block
+        b = x[: nb * block].reshape(nb, block).mean(axis=1)
+        return float(x.mean()), float(b.std(ddof=1) / np.sqrt(nb))
+
+    for beta in (2.0, 4.0):
+        row = {}
+        s = lqgpu.State(dim, L, 1.0, beta, lqgpu.PRECISION_F64)
+        s.set_links_random(11)
+        # the exponential link update keeps the links in SU(3) and the leap-frog reversible; the
+        # reference's first-order update drifts off the group at these step sizes, after which the
+        # Gauss projection fails
+        s.set_link_update(lqgpu.LINK_UPDATE_EXP)
+        uni = np.random.default_rng(int(beta * 100))
+        failed = 0
+
+        def traj(k, dt, n):
+            nonlocal failed
+            try:
+                return s.hmc_trajectory(dt, n, 13, k, float(uni.uniform()), max_gauss_steps=2001)["accepted"]
+            except lqgpu.LqError:  # the projection diverged or stalled: no proposal
+                failed += 1
+                return False
+        # the largest step (trajectory length 0.5) accepting >= 60% of 20 trial trajectories
+        k = 0
+        for dt in (0.04, 0.02, 0.01, 0.005):
+            n = int(round(0.5 / dt))
+            trial = [traj(k + i, dt, n) for i in range(20)]
+            k += 20
+            if np.mean(trial) >= 0.6:
+                break
+        plaq, acc = [], 0
+        for i in range(args.therm + args.meas):
+            a = traj(k, dt, n)
+            k += 1
+            if i >= args.therm:
+                plaq.append(s.average_trace_plaquette().real / 3.0)
+                acc += a
+        m, e = mean_err(plaq)
+        row["hmc"] = {"plaquette": m, "error": e, "acceptance": acc / args.meas, "dt": dt, "md_steps": n,
+                      "size": 1.0, "link_update": "exp", "trajectories": k, "failed_projections": failed,
+                      "finite": bool(np.isfinite(plaq).all())}
+        s.close()
+        s = lqgpu.State(dim, L, 1.0, beta, lqgpu.PRECISION_F64)
+        s.set_links_random(11)
+        plaq, pm = [], []
+        for k in range(args.therm + args.meas):
+            a, p = s.metropolis_sweep(4, 0.3, 17, k)
+            if k >= args.therm:
+                plaq.append(s.average_trace_plaquette().real / 3.0)
+                pm.append(p)
+        m, e = mean_err(plaq)
+        row["metropolis"] = {"plaquette": m, "error": e, "mean_acceptance_probability": float(np.mean(pm)),
+                             "sweeps": args.therm + args.meas, "n_update": 4, "spread": 0.3}
+        s.close()
+        d = row["hmc"]["plaquette"] - row["metropolis"]["plaquette"]
+        row["difference_in_sigma"] = d / np.hypot(row["hmc"]["error"], row["metropolis"]["error"])
+        out["betas"][str(beta)] = row
+        print(json.dumps({"beta": beta, **row}), flush=True)
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "scale", "batch", "adjoint"])
+    ap.add_argument("study", choices=["precision", "scale", "batch", "adjoint", "distribution"])
     ap.add_argument("--traj", type=int, default=None)
     ap.add_argument("--L", type=int, default=32)
     ap.add_argument("--betas", type=float, nargs="*", default=[0.5, 1.0, 2.0, 4.0])
     ap.add_argument("--quick", action="store_true", help="batch: skip the one-after-another comparison")
     ap.add_argument("--ensembles", type=int, default=64, help="batch: number of ensembles (the first n draws)")
+    ap.add_argument("--therm", type=int, default=200, help="distribution: thermalisation steps")
+    ap.add_argument("--meas", type=int, default=800, help="distribution: measured steps")
     ap.add_argument("--eager", action="store_true",
                     help="batch: launch the kernels one by one instead of the captured graph (for profilers, "
                          "which do not see kernels of graphs with conditional nodes)")
@@ -338,6 +417,8 @@ def main():
     elif args.study == "batch":
         args.traj = args.traj or 50
         res = batch_study(args)
+    elif args.study == "distribution":
+        res = distribution_study(args)
     else:
         if args.L == 32:
             args.L = 48

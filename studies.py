@@ -322,16 +322,18 @@ def adjoint_study(args):
 
 
 def distribution_study(args):
-    """Two samplers of the same Wilson measure exp(-beta sum (1 - Re Tr P / 3)) on the device: HMC
-    with the exponential link update (the reference's molecular dynamics carries no beta; momenta
-    N(0, 0.5/beta) make the links' marginal the Wilson measure) and checkerboard Metropolis.  D = 4, 8^4, beta 2 and 4 (smaller betas
+    """Samplers of the Wilson measure exp(-beta sum (1 - Re Tr P / 3)) on the device: checkerboard
+    Metropolis; the reference's HMC (momenta N(0, 0.5/beta) projected to the Gauss law, here with the
+    exponential link update); and standard HMC with momenta from the kinetic term of the reference's
+    own H, exp(-beta sum e^2 / 2), unprojected.  D = 4, 8^4, beta 2 and 4 (smaller betas
     give momenta for which the reference's Gauss projection diverges), random start; the average plaquette <Re Tr P>/3 over the measured part of each chain, with its error
     from blocks of 20 measurements."""
     dim, L = 4, 8
     out = {"study": "distribution", "dim": dim, "L": L, "betas": {}}
 
-    def mean_err(x, block=20):
+    def mean_err(x, block=None):
         x = np.asarray(x)
+        block = block or max(20, len(x) // 40)  # 40 blocks
         nb = len(x) // block
         b = x[: nb * block].reshape(nb, block).mean(axis=1)
         return float(x.mean()), float(b.std(ddof=1) / np.sqrt(nb))
@@ -374,6 +376,25 @@ def distribution_study(args):
                       "size": 1.0, "link_update": "exp", "trajectories": k, "failed_projections": failed,
                       "finite": bool(np.isfinite(plaq).all())}
         s.close()
+        # standard HMC: momenta from exp(-beta sum e^2 / 2), the kinetic term of the reference's H
+        # (std 1/sqrt(beta), not the 0.5/beta of new_random_e_state), no Gauss projection
+        s = lqgpu.State(dim, L, 1.0, beta, lqgpu.PRECISION_F64)
+        s.set_links_random(11)
+        s.set_link_update(lqgpu.LINK_UPDATE_EXP)
+        rng = np.random.default_rng(int(beta * 1000))
+        plaq, acc = [], 0
+        for i in range(args.therm + args.meas):
+            s.set_e_field(rng.normal(0.0, 1.0 / np.sqrt(beta), size=(L ** dim, dim, 8)))
+            p, h0, h1 = s.hmc_propose(dt, n)
+            a = p >= 1.0 or rng.uniform() < p
+            s.hmc_decide(a)
+            if i >= args.therm:
+                plaq.append(s.average_trace_plaquette().real / 3.0)
+                acc += a
+        m, e = mean_err(plaq)
+        row["hmc_standard_momenta"] = {"plaquette": m, "error": e, "acceptance": acc / args.meas, "dt": dt,
+                                       "md_steps": n, "momentum_std_dev": 1.0 / np.sqrt(beta)}
+        s.close()
         s = lqgpu.State(dim, L, 1.0, beta, lqgpu.PRECISION_F64)
         s.set_links_random(11)
         plaq, pm = [], []
@@ -386,8 +407,9 @@ def distribution_study(args):
         row["metropolis"] = {"plaquette": m, "error": e, "mean_acceptance_probability": float(np.mean(pm)),
                              "sweeps": args.therm + args.meas, "n_update": 4, "spread": 0.3}
         s.close()
-        d = row["hmc"]["plaquette"] - row["metropolis"]["plaquette"]
-        row["difference_in_sigma"] = d / np.hypot(row["hmc"]["error"], row["metropolis"]["error"])
+        for name in ("hmc", "hmc_standard_momenta"):
+            d = row[name]["plaquette"] - row["metropolis"]["plaquette"]
+            row[name]["vs_metropolis_sigma"] = d / np.hypot(row[name]["error"], row["metropolis"]["error"])
         out["betas"][str(beta)] = row
         print(json.dumps({"beta": beta, **row}), flush=True)
     print(json.dumps(out), flush=True)

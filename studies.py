@@ -325,9 +325,9 @@ def distribution_study(args):
     """Samplers of the Wilson measure exp(-beta sum (1 - Re Tr P / 3)) on the device: checkerboard
     Metropolis; the reference's HMC (momenta N(0, 0.5/beta) projected to the Gauss law, here with the
     exponential link update); and standard HMC with momenta from the kinetic term of the reference's
-    own H, exp(-beta sum e^2 / 2), unprojected.  D = 4, 8^4, beta 2 and 4 (smaller betas
-    give momenta for which the reference's Gauss projection diverges), random start; the average plaquette <Re Tr P>/3 over the measured part of each chain, with its error
-    from blocks of 20 measurements."""
+    own H, exp(-beta sum e^2 / 2), unprojected.  D = 4, 8^4, beta 2 and 4 (smaller betas give
+    momenta for which the reference's Gauss projection diverges), random start; the average
+    plaquette <Re Tr P>/3 over the measured part of each chain, with its error from 40 blocks."""
     dim, L = 4, 8
     out = {"study": "distribution", "dim": dim, "L": L, "betas": {}}
 

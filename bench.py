@@ -365,7 +365,8 @@ def run_ours(args):
             t = torch.empty(shape, dtype=torch.float64, pin_memory=True)
             t.normal_(0.0, 0.5 / beta, generator=torch.Generator().manual_seed(5 + j))
             host_bufs.append(t.numpy())
-        s.hmc_refresh_upload(host_bufs[0])  # warm the staging buffer
+        s.efield_prefetch(host_bufs[0])  # warm the prefetch buffer and copy stream
+        s.hmc_refresh_prefetched()
         s.hmc_propose(dt, nmd)
         s.hmc_decide(True)
         barrier()
@@ -373,8 +374,12 @@ def run_ours(args):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         d2h = 0
+        # momenta of trajectory k + 1 are copied while trajectory k runs (lq_efield_prefetch)
+        s.efield_prefetch(host_bufs[0])
         for k in range(args.e2e_steps):
-            steps = s.hmc_refresh_upload(host_bufs[k % 2])
+            steps = s.hmc_refresh_prefetched()
+            if k + 1 < args.e2e_steps:
+                s.efield_prefetch(host_bufs[(k + 1) % 2])
             p, h0, h1 = s.hmc_propose(dt, nmd)
             s.hmc_decide(p >= 1.0 or float(uni.uniform()) < p)
             plaq = s.average_trace_plaquette()
@@ -385,8 +390,9 @@ def run_ours(args):
         e2e_ms = max_over_ranks(ev0.elapsed_time(ev1))
         e2e = {"value": sum_over_ranks(n_links * nmd * args.e2e_steps) / (e2e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": int(np.prod(shape) * 8), "d2h_bytes_per_step": int(d2h / args.e2e_steps),
-               "path": "lq_hmc_refresh_upload + lq_hmc_propose + lq_hmc_decide + lq_average_trace_plaquette, "
-                       "momenta (f64, reference layout) from pinned host memory each trajectory"}
+               "path": "lq_efield_prefetch + lq_hmc_refresh_prefetched + lq_hmc_propose + lq_hmc_decide + "
+                       "lq_average_trace_plaquette, momenta (f64, reference layout) from pinned host memory each "
+                       "trajectory, the next trajectory's copy overlapping the current one"}
     plaq_mixed = s.average_trace_plaquette()
     s.close()
 

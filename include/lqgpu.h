@@ -245,6 +245,15 @@ int lq_leapfrog_adjoint(lq_state *s, double dt, int n_steps, int checkpoint_ever
 int lq_hmc_refresh(lq_state *s, uint64_t seed, uint64_t counter, int max_gauss_steps, int *gauss_steps);
 int lq_hmc_refresh_upload(lq_state *s, const double *efield_raw, size_t n_doubles, int max_gauss_steps,
                           int *gauss_steps);
+/* Pipelined test mode (no counterpart in the reference): lq_efield_prefetch starts the host -> device
+ * copy of the next trajectory's drawn momenta on a copy stream of the state and returns at once;
+ * lq_hmc_refresh_prefetched then does what lq_hmc_refresh_upload does with them.  Overlapping the
+ * copy of trajectory k+1 with the work of trajectory k hides it.  The host buffer must stay valid and
+ * unchanged until the lq_hmc_refresh_prefetched that consumes it returns; page-locked (pinned) host
+ * memory makes the copy asynchronous.  lq_hmc_refresh_prefetched without a prefetch returns
+ * LQ_ERR_NO_PENDING. */
+int lq_efield_prefetch(lq_state *s, const double *efield_raw, size_t n_doubles);
+int lq_hmc_refresh_prefetched(lq_state *s, int max_gauss_steps, int *gauss_steps);
 int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_old, double *h_new);
 int lq_hmc_decide(lq_state *s, int accept);
 int lq_hmc_trajectory(lq_state *s, double dt, int n_steps, uint64_t seed, uint64_t counter, double uniform,

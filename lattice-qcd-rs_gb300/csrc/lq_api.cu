@@ -112,6 +112,10 @@ void free_state(State *s) {
     if (s->d_out) cudaFree(s->d_out);
     if (s->h_out) cudaFreeHost(s->h_out);
     if (s->staging) cudaFree(s->staging);
+    if (s->prefetch) cudaFree(s->prefetch);
+    if (s->prefetch_done) cudaEventDestroy(s->prefetch_done);
+    if (s->prefetch_free) cudaEventDestroy(s->prefetch_free);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     delete static_cast<lq_state *>(s);
 }
 
@@ -911,6 +915,47 @@ int lq_hmc_refresh_upload(lq_state *s, const double *efield_raw, size_t n, int m
     if (!valid_std_dev(0.5 / s->beta)) return LQ_ERR_INVALID_NORMAL;
     int rc = lq_efield_upload(s, efield_raw, n);
     if (rc) return rc;
+    s->leap = 0;
+    s->t = 0;
+    return project_gauss(*s, max_gauss_steps, gauss_steps);
+}
+
+int lq_efield_prefetch(lq_state *s, const double *efield_raw, size_t n) {
+    LQ_CHECK_STATE(s);
+    if (!efield_raw) return LQ_ERR_INVALID_ARGUMENT;
+    if (n != (size_t)s->V * s->dim * 8) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n * sizeof(double);
+    if (!s->copy_stream) {
+        LQ_CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        LQ_CK(cudaEventCreateWithFlags(&s->prefetch_done, cudaEventDisableTiming));
+        LQ_CK(cudaEventCreateWithFlags(&s->prefetch_free, cudaEventDisableTiming));
+        LQ_CK(cudaEventRecord(s->prefetch_free, s->stream));
+    }
+    if (s->prefetch_bytes < bytes) {
+        LQ_CK(cudaStreamSynchronize(s->copy_stream));
+        if (s->prefetch) LQ_CK(cudaFree(s->prefetch));
+        s->prefetch = nullptr;
+        s->prefetch_bytes = 0;
+        LQ_CK(cudaMalloc(&s->prefetch, bytes));
+        s->prefetch_bytes = bytes;
+    }
+    // the copy may overwrite the buffer only once its previous contents have been converted
+    LQ_CK(cudaStreamWaitEvent(s->copy_stream, s->prefetch_free, 0));
+    LQ_CK(cudaMemcpyAsync(s->prefetch, efield_raw, bytes, cudaMemcpyHostToDevice, s->copy_stream));
+    LQ_CK(cudaEventRecord(s->prefetch_done, s->copy_stream));
+    s->prefetch_pending = 1;
+    return LQ_OK;
+}
+
+int lq_hmc_refresh_prefetched(lq_state *s, int max_gauss_steps, int *gauss_steps) {
+    LQ_CHECK_STATE(s);
+    if (!s->prefetch_pending) return LQ_ERR_NO_PENDING;
+    if (!valid_std_dev(0.5 / s->beta)) return LQ_ERR_INVALID_NORMAL;
+    LQ_CK(cudaStreamWaitEvent(s->stream, s->prefetch_done, 0));
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_from_aos(*s, (const double *)s->prefetch));
+    LQ_CK(cudaEventRecord(s->prefetch_free, s->stream));
+    s->prefetch_pending = 0;
+    s->has_pending = 0;
     s->leap = 0;
     s->t = 0;
     return project_gauss(*s, max_gauss_steps, gauss_steps);

@@ -46,6 +46,13 @@ struct State {
     double *h_out = nullptr;    // pinned host mirror of d_out
     void *staging = nullptr;    // f64 AoS staging for uploads/downloads
     size_t staging_bytes = 0;
+    // momenta prefetch (lq_efield_prefetch): a second staging buffer filled on its own stream
+    void *prefetch = nullptr;
+    size_t prefetch_bytes = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t prefetch_done = nullptr; // the copy has landed
+    cudaEvent_t prefetch_free = nullptr; // the last prefetched field has been consumed
+    int prefetch_pending = 0;
 
     long long t = 0;
     int leap = 0;

@@ -71,6 +71,8 @@ SIGNATURES = {
     "lq_leapfrog_n": (_i32, [_vp, _f64, _i32]),
     "lq_hmc_refresh": (_i32, [_vp, _u64, _u64, _i32, _ip]),
     "lq_hmc_refresh_upload": (_i32, [_vp, _dp, _sz, _i32, _ip]),
+    "lq_efield_prefetch": (_i32, [_vp, _dp, _sz]),
+    "lq_hmc_refresh_prefetched": (_i32, [_vp, _i32, _ip]),
     "lq_hmc_propose": (_i32, [_vp, _f64, _i32, _dp, _dp, _dp]),
     "lq_hmc_decide": (_i32, [_vp, _i32]),
     "lq_hmc_trajectory": (_i32, [_vp, _f64, _i32, _u64, _u64, _f64, _i32, _ip, _dp, _dp, _ip]),
@@ -370,6 +372,22 @@ class State:
         steps = ctypes.c_int()
         _check(load().lq_hmc_refresh_upload(self._h, _p(a), a.size, max_gauss_steps, ctypes.byref(steps)),
                "lq_hmc_refresh_upload")
+        return steps.value
+
+    def efield_prefetch(self, efield_raw):
+        """start copying the next trajectory's raw momenta (keep the array alive and unchanged until
+        hmc_refresh_prefetched returns; pinned memory makes the copy asynchronous)"""
+        a = efield_raw
+        if a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise TypeError("expected a C-contiguous float64 array")
+        self._prefetched = a
+        _check(load().lq_efield_prefetch(self._h, _p(a), a.size), "lq_efield_prefetch")
+
+    def hmc_refresh_prefetched(self, max_gauss_steps=100000):
+        steps = ctypes.c_int()
+        _check(load().lq_hmc_refresh_prefetched(self._h, max_gauss_steps, ctypes.byref(steps)),
+               "lq_hmc_refresh_prefetched")
+        self._prefetched = None
         return steps.value
 
     def hmc_propose(self, dt, n_steps):

@@ -54,6 +54,15 @@ template <typename T> struct MinBlocks {
     static constexpr int md = sizeof(T) == 4 ? LQ_MD_MIN_BLOCKS : 1;
     static constexpr int sweep = sizeof(T) == 4 ? LQ_SWEEP_MIN_BLOCKS : 1;
 };
+// The single-lattice plaquette difference in FP32 at D = 4 fits three blocks per SM without
+// spilling (168 registers; two at the allocator's own choice of 172); D = 2, 3 and the batched
+// kernel spill under the same cap and keep the allocator's choice.
+#ifndef LQ_DELTA_MIN_BLOCKS
+#define LQ_DELTA_MIN_BLOCKS 3
+#endif
+template <int D, typename T> struct MinBlocksDelta {
+    static constexpr int value = (sizeof(T) == 4 && D == 4) ? LQ_DELTA_MIN_BLOCKS : 1;
+};
 
 // (hi, lo) += d: two-sum of hi and d, error folded into lo, pair renormalised
 // (Knuth's TwoSum followed by Dekker's FastTwoSum; no product, so nothing is contracted).
@@ -679,8 +688,8 @@ __device__ __forceinline__ double plaquette_delta_site(const V2<T> *__restrict__
     }
 }
 template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128) k_plaquette_delta(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un,
-                                                         Geo<D> g, double *__restrict__ partial) {
+__global__ void __launch_bounds__(128, (MinBlocksDelta<D, T>::value))
+    k_plaquette_delta(const V2<T> *__restrict__ Uo, const V2<T> *__restrict__ Un, Geo<D> g, double *__restrict__ partial) {
     const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (site < g.V)

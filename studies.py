@@ -1,6 +1,7 @@
 #!/usr/bin/env python
-"""Accuracy and scale studies of the HMC path on one GPU (the brief's precision and
-scale-sweep configurations), printing one JSON object per study.
+"""Accuracy and scale studies of the HMC path on one GPU (the precision and scale-sweep
+workloads), printing one JSON object per study.  --size sets the states' size parameter of the
+precision and scale studies (default 1000; "L" for size = side length).
 
 precision : D = 4, 32^4, beta in {0.5, 1, 2, 4}, random_su3 start (seed 1), 20 leap-frog steps
             dt 0.005, N trajectories per beta.  The FP64 form and each FP32-arithmetic form
@@ -8,7 +9,7 @@ precision : D = 4, 32^4, beta in {0.5, 1, 2, 4}, random_su3 start (seed 1), 20 l
             through lq_hmc_refresh_upload) and accept uniforms; reported per beta: max |Delta H
             error|, max |Delta <P>/3|, acceptance of each form, and the forward/backward
             reversibility of one trajectory (momenta flipped at the end, integrated back).
-            Mixed reprojects its links (FP64) every 10 trajectories.  Where the Gauss projection
+            Every form reprojects its links onto SU(3) every 10 trajectories.  Where the Gauss projection
             of the momenta fails (the reference's relaxation diverges to NaN for momentum
             standard deviations near 1, i.e. beta = 0.5), the beta records the failure.
 scale     : D = 4 at 24^4, 32^4, 48^4, 64^4 and D = 3 at 128^3, 256^3, beta 2, seed 4, 20 steps
@@ -25,7 +26,7 @@ adjoint   : d<plaq>/dbeta through a 50-step leap-frog at 48^4 by the checkpointe
 distribution: HMC and checkerboard Metropolis on the same lattice and beta give the same average
             plaquette within statistical errors (both sample the Wilson measure).
 
-usage: python studies.py precision [--traj N] | scale [--traj K] | batch [--traj N] | adjoint [--L 48]
+usage: python studies.py precision [--traj N] [--size L] | scale [--traj K] [--size L] | batch [--traj N] | adjoint [--L 48]
        | distribution [--therm N --meas M]
 """
 import argparse
@@ -52,8 +53,15 @@ def hbm_peak():
         return 6800.0
 
 
+def study_size(args, L):
+    """The `size` parameter of the states: a number, or "L" for size = side length (the links and
+    momenta then move L times farther per step than at the default size 1000 / L)."""
+    return float(L) if args.size == "L" else float(args.size)
+
+
 def precision_study(args):
-    dim, L, size, dt, nmd = 4, args.L, 1000.0, 0.005, 20
+    dim, L, dt, nmd = 4, args.L, 0.005, 20
+    size = study_size(args, L)
     out = {"study": "precision", "dim": dim, "L": L, "size": size, "dt": dt, "md_steps": nmd,
            "trajectories_per_beta": args.traj, "betas": {}}
     forms = [lqgpu.PRECISION_F64, lqgpu.PRECISION_MIXED, lqgpu.PRECISION_F32]
@@ -87,7 +95,7 @@ def precision_study(args):
                 s.hmc_decide(a)
                 acc[p] += a
                 res[p] = (h1 - h0, s.average_trace_plaquette().real / 3.0)
-                if p == lqgpu.PRECISION_MIXED and (k + 1) % 10 == 0:
+                if (k + 1) % 10 == 0:
                     s.normalize_link_matrices()
             if failure:
                 break
@@ -148,12 +156,14 @@ def time_trajectories(state, k, dt, nmd, warm=1):
 
 
 def scale_study(args):
-    dt, nmd, beta, size = 0.005, 20, 2.0, 1000.0
+    dt, nmd, beta = 0.005, 20, 2.0
     peak = hbm_peak()
-    out = {"study": "scale", "beta": beta, "dt": dt, "md_steps": nmd, "trajectories": args.traj, "lattices": []}
+    out = {"study": "scale", "beta": beta, "dt": dt, "md_steps": nmd, "trajectories": args.traj,
+           "size": args.size, "lattices": []}
     for dim, L in ((4, 24), (4, 32), (4, 48), (4, 64), (3, 128), (3, 256)):
+        size = study_size(args, L)
         n_links = L ** dim * dim
-        row = {"dim": dim, "L": L, "links": n_links}
+        row = {"dim": dim, "L": L, "links": n_links, "size": size}
         for p in (lqgpu.PRECISION_MIXED, lqgpu.PRECISION_F64):
             k = args.traj if p != lqgpu.PRECISION_F64 else max(1, args.traj // 5)
             s = lqgpu.State(dim, L, size, beta, p)
@@ -422,6 +432,8 @@ def main():
     ap.add_argument("--traj", type=int, default=None)
     ap.add_argument("--L", type=int, default=32)
     ap.add_argument("--betas", type=float, nargs="*", default=[0.5, 1.0, 2.0, 4.0])
+    ap.add_argument("--size", default="1000",
+                    help="precision, scale: the states' size parameter, a number or L for size = side length")
     ap.add_argument("--quick", action="store_true", help="batch: skip the one-after-another comparison")
     ap.add_argument("--ensembles", type=int, default=64, help="batch: number of ensembles (the first n draws)")
     ap.add_argument("--therm", type=int, default=200, help="distribution: thermalisation steps")

@@ -3,7 +3,7 @@ lq_wilson_action_backward): against the reference's force (derivative_e,
 src/simulation/state.rs:1420-1448, through the oracle) and against central finite differences
 of the action along all 8 generators.
 
-Finite-difference configuration (the brief's differentiation case): D = 4, 16^4, beta 2,
+Finite-difference configuration (the differentiation workload): D = 4, 16^4, beta 2,
 random links (seed 2), FP64, eps = 1e-5, 1024 random links x 8 generators.  The action is a sum
 of ~4e5 plaquette terms, so S itself carries ~1e-10 of rounding; the difference quotient is
 therefore compared with a 1e-4 absolute tolerance (the gradient entries are O(1)).

@@ -25,8 +25,9 @@ constexpr uint32_t kChunk = 128; // sites per chunk = threads per block of the b
 
 // per ensemble, constant after creation (device copy)
 struct BatchEns {
-    uint32_t V, L, tile0, chunk0, nchunks, pad;
+    uint32_t V, L, tile0, chunk0, nchunks, ls;
     uint32_t stride[4];
+    uint32_t lm, pad; // division by L (divisor_magic: multiplier lm, shift ls)
     double size, beta;
     // coefficients in the single-lattice path's arithmetic (Engine::md, Engine::efield_normal),
     // computed on the host in double and stored in both storage types so that no kernel needs

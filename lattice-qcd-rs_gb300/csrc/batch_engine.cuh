@@ -42,6 +42,8 @@ template <int D> __device__ __forceinline__ Geo<D> geo_of(const BatchEns &e) {
     g.L = e.L;
 #pragma unroll
     for (int i = 0; i < 4; ++i) g.stride[i] = e.stride[i];
+    g.lm = e.lm;
+    g.ls = e.ls;
     return g;
 }
 
@@ -371,13 +373,7 @@ template <int D, typename T, bool COMP> struct BatchEngine {
     // per-ensemble element offsets
     static size_t ub(const Batch &b, int e) { return (size_t)b.ens_h[e].tile0 * (D * 9 * kTile); }
     static dim3 link_grid(const Batch &b, int e) { return dim3((b.ens_h[e].V + 127) / 128, D, 1); }
-    static Geo<D> geo_h(const Batch &b, int e) {
-        Geo<D> g;
-        g.V = b.ens_h[e].V;
-        g.L = b.ens_h[e].L;
-        for (int i = 0; i < 4; ++i) g.stride[i] = b.ens_h[e].stride[i];
-        return g;
-    }
+    static Geo<D> geo_h(const Batch &b, int e) { return make_geo<D>(b.ens_h[e].V, b.ens_h[e].L); }
     // per-ensemble operations on link buffer `buf` (the ensemble's state buffer, run[e].cur)
     static cudaError_t links_from_aos(Batch &b, int e, int buf, const double *d_aos) {
         k_links_from_aos<D, T, COMP><<<link_grid(b, e), 128, 0, b.stream>>>(d_aos, (V2<T> *)b.U[buf] + ub(b, e),

@@ -10,17 +10,7 @@
 namespace lq {
 
 template <int D, typename T, bool COMP> struct Engine {
-    static Geo<D> geo(const State &s) {
-        Geo<D> g;
-        g.V = s.V;
-        g.L = (uint32_t)s.L;
-        uint32_t st = 1;
-        for (int i = 0; i < 4; ++i) {
-            g.stride[i] = st;
-            if (i < D) st *= (uint32_t)s.L;
-        }
-        return g;
-    }
+    static Geo<D> geo(const State &s) { return make_geo<D>(s.V, (uint32_t)s.L); }
     static dim3 link_grid(const State &s, int threads) { return dim3((s.V + threads - 1) / threads, D, 1); }
     // distance in elements from the hi array to the lo array of compensated links / E-field
     static size_t ulo(const State &s) { return (size_t)tiles_of(s.V) * D * 9 * kTile; }

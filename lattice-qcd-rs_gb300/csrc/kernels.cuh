@@ -21,11 +21,45 @@ template <int D> struct Geo {
     uint32_t V;         // number of sites L^D
     uint32_t L;         // points per direction
     uint32_t stride[4]; // L^mu
+    uint32_t lm, ls;    // division by L: n / L = (mulhi(n, lm) + n) >> ls (divisor_magic)
 };
 
+// Multiplier m and shift s of the division by d >= 1 for every 32-bit dividend n, by the round-up
+// method of Granlund and Montgomery ("Division by invariant integers using multiplication", 1994):
+// s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1, n / d = (mulhi(n, m) + n) >> s with the
+// sum taken in 64 bits.  A few integer instructions instead of the general division.
+__host__ __device__ inline void divisor_magic(uint32_t d, uint32_t &m, uint32_t &s) {
+    s = 0;
+    while ((1ull << s) < d) ++s;
+    m = (uint32_t)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+}
+
+template <int D> __host__ __device__ inline Geo<D> make_geo(uint32_t V, uint32_t L) {
+    Geo<D> g;
+    g.V = V;
+    g.L = L;
+    uint32_t st = 1;
+    for (int i = 0; i < 4; ++i) {
+        g.stride[i] = st;
+        if (i < D) st *= L;
+    }
+    divisor_magic(L, g.lm, g.ls);
+    return g;
+}
+
+template <int D> __device__ __forceinline__ uint32_t div_by_L(const Geo<D> &g, uint32_t n) {
+    return (uint32_t)(((uint64_t)__umulhi(n, g.lm) + n) >> g.ls);
+}
+
+// coordinates of a site, c[i] = (site / L^i) % L, one division by L per direction
 template <int D> __device__ __forceinline__ void site_coords(const Geo<D> &g, uint32_t site, uint32_t *c) {
+    uint32_t r = site;
 #pragma unroll
-    for (int i = 0; i < D; ++i) c[i] = (site / g.stride[i]) % g.L;
+    for (int i = 0; i < D; ++i) {
+        const uint32_t q = div_by_L(g, r);
+        c[i] = r - q * g.L;
+        r = q;
+    }
 }
 // neighbour of `site` (whose coordinate along mu is cmu) in +mu / -mu, periodic
 template <int D>
@@ -64,17 +98,52 @@ template <int D, typename T> struct MinBlocksDelta {
     static constexpr int value = (sizeof(T) == 4 && D == 4) ? LQ_DELTA_MIN_BLOCKS : 1;
 };
 
-// (hi, lo) += d: two-sum of hi and d, error folded into lo, pair renormalised
-// (Knuth's TwoSum followed by Dekker's FastTwoSum; no product, so nothing is contracted).
+// a + b and a - b rounded to nearest, never fused with a product that computed an operand
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// (hi, lo) += d: two-sum of hi and d, error folded into lo, pair renormalised (Knuth's TwoSum
+// followed by Dekker's FastTwoSum).  Every add is an explicit rounded add: d is usually a product
+// (k f, drift x), and an add contracted with it into an FMA would break the two-sum's exactness.
 template <typename T> __device__ __forceinline__ void comp_add(T &hi, T &lo, T d) {
-    const T s = hi + d;
-    const T bb = s - hi;
-    const T err = (hi - (s - bb)) + (d - bb);
-    const T l = lo + err;
-    const T h = s + l;
-    lo = l - (h - s);
+    const T s = add_rn(hi, d);
+    const T bb = sub_rn(s, hi);
+    const T err = add_rn(sub_rn(hi, sub_rn(s, bb)), sub_rn(d, bb));
+    const T l = add_rn(lo, err);
+    const T h = add_rn(s, l);
+    lo = sub_rn(l, sub_rn(h, s));
     hi = h;
 }
+// Two independent compensated adds, (h0, l0) += d0 and (h1, l1) += d1 (the real and imaginary
+// parts of one entry, or two momentum components).  With LQ_PAIRED_ADD (the default) the FP32 form
+// runs both lanes through the paired FP32 adds of sm_100 and later (__fadd2_rn), each lane rounding
+// exactly as comp_add rounds it: bitwise the same results, 12 us less per k_md launch at 32^4.
+#ifndef LQ_PAIRED_ADD
+#define LQ_PAIRED_ADD 1
+#endif
+template <typename T> __device__ __forceinline__ void comp_add2(T &h0, T &h1, T &l0, T &l1, T d0, T d1) {
+    comp_add(h0, l0, d0);
+    comp_add(h1, l1, d1);
+}
+#if LQ_PAIRED_ADD
+__device__ __forceinline__ float2 neg2(float2 x) { return make_float2(-x.x, -x.y); }
+template <>
+__device__ __forceinline__ void comp_add2<float>(float &h0, float &h1, float &l0, float &l1, float d0, float d1) {
+    const float2 hi = make_float2(h0, h1), lo = make_float2(l0, l1), d = make_float2(d0, d1);
+    const float2 s = __fadd2_rn(hi, d);
+    const float2 bb = __fadd2_rn(s, neg2(hi));
+    const float2 err = __fadd2_rn(__fadd2_rn(hi, neg2(__fadd2_rn(s, neg2(bb)))), __fadd2_rn(d, neg2(bb)));
+    const float2 l = __fadd2_rn(lo, err);
+    const float2 h = __fadd2_rn(s, l);
+    const float2 nl = __fadd2_rn(l, neg2(__fadd2_rn(h, neg2(s))));
+    h0 = h.x;
+    h1 = h.y;
+    l0 = nl.x;
+    l1 = nl.y;
+}
+#endif
 // split a double into a pair of T (exact for T = double with lo = 0)
 template <typename T> __device__ __forceinline__ void split(double x, T &hi, T &lo) {
     hi = (T)x;
@@ -191,12 +260,16 @@ __device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *ou, c
     if (MODE & MD_KICK) {
         T f[8];
         im_tr_generators_of_product(u, sig, f);
+        if (COMP) {
+            // compensated storage: one exact-sum update with both half-kicks (the separate
+            // adds of the FP64 form only reproduce the reference's FP64 rounding)
+            const T k = k1 + k2;
+#pragma unroll
+            for (int a = 0; a < 8; a += 2) comp_add2(e[a], e[a + 1], el[a], el[a + 1], k * f[a], k * f[a + 1]);
+        }
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
             if (COMP) {
-                // compensated storage: one exact-sum update with both half-kicks (the separate
-                // adds of the FP64 form only reproduce the reference's FP64 rounding)
-                comp_add(e[a], el[a], (k1 + k2) * f[a]);
                 Eout[elo + ei + a * kTile] = el[a];
             } else {
                 if (k1 != T(0)) e[a] = fma(k1, f[a], e[a]);
@@ -233,8 +306,7 @@ __device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *ou, c
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
             if (COMP) {
-                comp_add(u.e[k].re, ul.e[k].re, w.e[k].re);
-                comp_add(u.e[k].im, ul.e[k].im, w.e[k].im);
+                comp_add2(u.e[k].re, u.e[k].im, ul.e[k].re, ul.e[k].im, w.e[k].re, w.e[k].im);
             } else {
                 u.e[k].re += w.e[k].re;
                 u.e[k].im += w.e[k].im;
@@ -411,10 +483,10 @@ template <typename T, bool COMP>
 __device__ __forceinline__ void projection_step(const mat3<T> &u, const mat3<T> &gx, const T *gxc, const mat3<T> &gp,
                                                 T *e, T *el) {
     mat3<T> t1, t2;
-    mul_nn(u, gx, t1);
+    mul_nh(u, gx, t1);      // G(x) Hermitian
     mul_na_herm(t1, u, t2); // u G(x) u^dag is Hermitian
     T xc[8];
-    two_re_tr_generators_of_product(t2, gp, xc);
+    two_re_tr_generators_of_hermitian_product(t2, gp, xc);
     const T K = T(0.12);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {

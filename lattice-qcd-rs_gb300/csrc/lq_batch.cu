@@ -365,6 +365,7 @@ int lq_batch_create(int dim, int n_ensembles, const int *L, const double *size, 
             en.stride[i] = st;
             if (i < dim) st *= (uint32_t)L[e];
         }
+        lq::divisor_magic(en.L, en.lm, en.ls);
         en.tile0 = (uint32_t)tiles;
         en.chunk0 = (uint32_t)chunks;
         en.nchunks = (uint32_t)((V + lq::kChunk - 1) / lq::kChunk);

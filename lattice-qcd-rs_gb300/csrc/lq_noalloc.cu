@@ -117,21 +117,9 @@ __global__ void __launch_bounds__(kBlock) k_plaquette_aos(const double *__restri
     lq::block_reduce_store<3>(v, partial, blockIdx.x, gridDim.x);
 }
 
-template <int D> Geo<D> make_geo(uint32_t V, int L) {
-    Geo<D> g;
-    g.V = V;
-    g.L = (uint32_t)L;
-    uint32_t st = 1;
-    for (int i = 0; i < 4; ++i) {
-        g.stride[i] = st;
-        if (i < D) st *= (uint32_t)L;
-    }
-    return g;
-}
-
 template <int D> cudaError_t launch(const double *links, uint32_t V, int L, double *scratch, double *out, cudaStream_t st) {
     const uint32_t blocks = (V + kBlock - 1) / kBlock;
-    k_plaquette_aos<D><<<blocks, kBlock, 0, st>>>(links, make_geo<D>(V, L), scratch);
+    k_plaquette_aos<D><<<blocks, kBlock, 0, st>>>(links, lq::make_geo<D>(V, (uint32_t)L), scratch);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     lq::k_finalize<3><<<1, 1024, 0, st>>>(scratch, blocks, out);

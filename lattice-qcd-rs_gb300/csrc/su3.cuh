@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace lq {
 
 template <typename T> struct cpx {
@@ -57,6 +59,56 @@ template <typename T> __device__ __forceinline__ void mul_nn(const mat3<T> &a, c
                 im = fma(a.e[i * 3 + k].re, b.e[k * 3 + j].im, im);
                 im = fma(a.e[i * 3 + k].im, b.e[k * 3 + j].re, im);
             }
+            r.e[i * 3 + j] = cmk(re, im);
+        }
+}
+
+// One complex multiply-add term of mul_nn, with AR / BR telling that a / b is known to be real
+// (the diagonal of a Hermitian matrix, whose imaginary part is an exact zero): the multiply-adds
+// with that zero are left out.  fma(x, 0, y) returns y, so every nonzero result rounds as the
+// full term rounds it (only the sign of an exact zero can differ).
+//   cmul_first: re = a.re b.re - a.im b.im, im = a.re b.im + a.im b.re (mul_nn's k = 0 term)
+//   cmul_acc  : re += a.re b.re - a.im b.im, im += a.re b.im + a.im b.re, in mul_nn's order
+template <bool AR, bool BR, typename T>
+__device__ __forceinline__ void cmul_first(const cpx<T> &a, const cpx<T> &b, T &re, T &im) {
+    if constexpr (AR && BR) {
+        re = a.re * b.re;
+        im = T(0);
+    } else if constexpr (AR) {
+        re = a.re * b.re;
+        im = a.re * b.im;
+    } else if constexpr (BR) {
+        re = a.re * b.re;
+        im = a.im * b.re;
+    } else {
+        re = a.re * b.re;
+        im = a.re * b.im;
+        re = fma(-a.im, b.im, re);
+        im = fma(a.im, b.re, im);
+    }
+}
+template <bool AR, bool BR, typename T>
+__device__ __forceinline__ void cmul_acc(const cpx<T> &a, const cpx<T> &b, T &re, T &im) {
+    re = fma(a.re, b.re, re);
+    if constexpr (!AR && !BR) re = fma(-a.im, b.im, re);
+    if constexpr (!BR) im = fma(a.re, b.im, im);
+    if constexpr (!AR) im = fma(a.im, b.re, im);
+}
+
+// r = a * g for g Hermitian with a real diagonal (as herm_load builds it): mul_nn less the 18
+// multiply-adds with the zero imaginary parts of g's diagonal.
+template <typename T> __device__ __forceinline__ void mul_nh(const mat3<T> &a, const mat3<T> &g, mat3<T> &r) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            T re, im;
+            if (j == 0) cmul_first<false, true>(a.e[i * 3], g.e[j], re, im);
+            else cmul_first<false, false>(a.e[i * 3], g.e[j], re, im);
+            if (j == 1) cmul_acc<false, true>(a.e[i * 3 + 1], g.e[3 + j], re, im);
+            else cmul_acc<false, false>(a.e[i * 3 + 1], g.e[3 + j], re, im);
+            if (j == 2) cmul_acc<false, true>(a.e[i * 3 + 2], g.e[6 + j], re, im);
+            else cmul_acc<false, false>(a.e[i * 3 + 2], g.e[6 + j], re, im);
             r.e[i * 3 + j] = cmk(re, im);
         }
 }
@@ -277,6 +329,47 @@ __device__ __forceinline__ void two_re_tr_generators_of_product(const mat3<T> &a
     const cpx<T> x1 = entry(0, 1), x3 = entry(1, 0), x2 = entry(0, 2), x6 = entry(2, 0), x5 = entry(1, 2),
                  x7 = entry(2, 1);
     const T x0 = diag_re(0), x4 = diag_re(1), x8 = diag_re(2);
+    out[0] = x3.re + x1.re;
+    out[1] = x3.im - x1.im;
+    out[2] = x0 - x4;
+    out[3] = x6.re + x2.re;
+    out[4] = x6.im - x2.im;
+    out[5] = x7.re + x5.re;
+    out[6] = x7.im - x5.im;
+    out[7] = T(2.0 * kOneOver2Sqrt3) * (x0 + x4) + T(2.0 * kMinusOneOverSqrt3) * x8;
+}
+
+// out^a = 2 Re Tr(T^a a b) for a and b both Hermitian with real diagonals (u G u^dag and G in the
+// projection step): two_re_tr_generators_of_product less the 27 multiply-adds with the zero
+// imaginary parts of the two diagonals (63 instead of 90).
+template <typename T>
+__device__ __forceinline__ void two_re_tr_generators_of_hermitian_product(const mat3<T> &a, const mat3<T> &b, T *out) {
+    // entry (i, j), i != j, of a b: a's term k is real for k == i, b's for k == j
+    auto entry = [&](auto ic, auto jc) {
+        constexpr int i = decltype(ic)::value, j = decltype(jc)::value;
+        T re, im;
+        cmul_first<i == 0, j == 0>(a.e[i * 3], b.e[j], re, im);
+        cmul_acc<i == 1, j == 1>(a.e[i * 3 + 1], b.e[3 + j], re, im);
+        cmul_acc<i == 2, j == 2>(a.e[i * 3 + 2], b.e[6 + j], re, im);
+        return cmk(re, im);
+    };
+    // real part of the diagonal entry (i, i)
+    auto diag_re = [&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        T re = a.e[i * 3].re * b.e[i].re;
+        if constexpr (i != 0) re = fma(-a.e[i * 3].im, b.e[i].im, re);
+        re = fma(a.e[i * 3 + 1].re, b.e[3 + i].re, re);
+        if constexpr (i != 1) re = fma(-a.e[i * 3 + 1].im, b.e[3 + i].im, re);
+        re = fma(a.e[i * 3 + 2].re, b.e[6 + i].re, re);
+        if constexpr (i != 2) re = fma(-a.e[i * 3 + 2].im, b.e[6 + i].im, re);
+        return re;
+    };
+    using I0 = std::integral_constant<int, 0>;
+    using I1 = std::integral_constant<int, 1>;
+    using I2 = std::integral_constant<int, 2>;
+    const cpx<T> x1 = entry(I0{}, I1{}), x3 = entry(I1{}, I0{}), x2 = entry(I0{}, I2{}), x6 = entry(I2{}, I0{}),
+                 x5 = entry(I1{}, I2{}), x7 = entry(I2{}, I1{});
+    const T x0 = diag_re(I0{}), x4 = diag_re(I1{}), x8 = diag_re(I2{});
     out[0] = x3.re + x1.re;
     out[1] = x3.im - x1.im;
     out[2] = x0 - x4;

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(128) k_adj_init(const V2<T> *__restrict__ U, V
     mat_adj(sig, r);
 #pragma unroll
     for (int k = 0; k < 9; ++k) r.e[k] = cmk(scale * r.e[k].re, scale * r.e[k].im);
-    store_mat<T>(lamU + tix(site, D * 9, mu * 9), r);
+    store_link<T>(lamU, tix(site, D * 9, mu * 9), r);
 }
 
 // one plaquette loop U_m X Y Z of link m: R of the loop (see the header comment).  Each of X,
@@ -96,7 +96,7 @@ template <int D, typename T>
 __device__ __forceinline__ void load_coef(const T *__restrict__ lamE, uint32_t site, int dir, T (&c)[8]) {
     const size_t ei = tix(site, D * 8, dir * 8);
 #pragma unroll
-    for (int a = 0; a < 8; ++a) c[a] = lamE[ei + a * kTile];
+    for (int a = 0; a < 8; ++a) c[a] = lamE[ei + efield_off<T>(ei, a)];
 }
 
 // lam_U(m) += coef * i * (sum over the 2(D-1) plaquette loops of m of R)^dag, coef = h c
@@ -124,9 +124,9 @@ __global__ void __launch_bounds__(128) k_adj_kick(const V2<T> *__restrict__ U, c
         {
             // upper loop: U_mu(x) U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag
             const uint32_t xpnu = fwd(g, site, c[nu], nu);
-            load_mat<T>(U + tix(xpmu, D * 9, nu * 9), u[0]);
-            load_mat<T>(U + tix(xpnu, D * 9, mu * 9), u[1]);
-            load_mat<T>(U + tix(site, D * 9, nu * 9), u[2]);
+            load_link<T>(U, tix(xpmu, D * 9, nu * 9), u[0]);
+            load_link<T>(U, tix(xpnu, D * 9, mu * 9), u[1]);
+            load_link<T>(U, tix(site, D * 9, nu * 9), u[2]);
             load_coef<D, T>(lamE, xpmu, nu, cl[0]);
             load_coef<D, T>(lamE, xpnu, mu, cl[1]);
             load_coef<D, T>(lamE, site, nu, cl[2]);
@@ -137,9 +137,9 @@ __global__ void __launch_bounds__(128) k_adj_kick(const V2<T> *__restrict__ U, c
             // lower loop: U_mu(x) U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)
             const uint32_t xmnu = bwd(g, site, c[nu], nu);
             const uint32_t xpmu_mnu = bwd(g, xpmu, c[nu], nu);
-            load_mat<T>(U + tix(xpmu_mnu, D * 9, nu * 9), u[0]);
-            load_mat<T>(U + tix(xmnu, D * 9, mu * 9), u[1]);
-            load_mat<T>(U + tix(xmnu, D * 9, nu * 9), u[2]);
+            load_link<T>(U, tix(xpmu_mnu, D * 9, nu * 9), u[0]);
+            load_link<T>(U, tix(xmnu, D * 9, mu * 9), u[1]);
+            load_link<T>(U, tix(xmnu, D * 9, nu * 9), u[2]);
             load_coef<D, T>(lamE, xpmu_mnu, nu, cl[0]);
             load_coef<D, T>(lamE, xmnu, mu, cl[1]);
             load_coef<D, T>(lamE, xmnu, nu, cl[2]);
@@ -148,17 +148,18 @@ __global__ void __launch_bounds__(128) k_adj_kick(const V2<T> *__restrict__ U, c
         }
     }
     // += coef * i * racc^dag: i (a - ib) = b + ia for each entry a + ib of racc^T
-    V2<T> *p = lamU + tix(site, D * 9, mu * 9);
+    const size_t ui = tix(site, D * 9, mu * 9);
+    mat3<T> l;
+    load_link<T>(lamU, ui, l);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             const cpx<T> r = racc.e[j * 3 + i];
-            V2<T> v = p[(i * 3 + j) * kTile];
-            v.x = fma(coef, r.im, v.x);
-            v.y = fma(coef, r.re, v.y);
-            p[(i * 3 + j) * kTile] = v;
+            l.e[i * 3 + j].re = fma(coef, r.im, l.e[i * 3 + j].re);
+            l.e[i * 3 + j].im = fma(coef, r.re, l.e[i * 3 + j].im);
         }
+    store_link<T>(lamU, ui, l);
 }
 
 // adjoint of the drift U' = U + kappa i E U at the links U (before the drift) and momenta E:
@@ -172,21 +173,21 @@ __global__ void __launch_bounds__(128) k_adj_drift(const V2<T> *__restrict__ U, 
     if (site >= V) return;
     const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
     mat3<T> u, lu, lua, x;
-    load_mat<T>(U + ui, u);
-    load_mat<T>(lamU + ui, lu);
+    load_link<T>(U, ui, u);
+    load_link<T>(lamU, ui, lu);
     mat_adj(lu, lua);
     T f[8], e[8];
     im_tr_generators_of_product(u, lua, f);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        lamE[ei + a * kTile] = fma(-kappa, f[a], lamE[ei + a * kTile]);
-        e[a] = E[ei + a * kTile];
+        lamE[ei + efield_off<T>(ei, a)] = fma(-kappa, f[a], lamE[ei + efield_off<T>(ei, a)]);
+        e[a] = E[ei + efield_off<T>(ei, a)];
     }
     adj_mul<T>(e, lu, x); // E lam_U
     // -kappa i x: -i (a + ib) = b - ia
 #pragma unroll
     for (int k = 0; k < 9; ++k) lu.e[k] = cmk(fma(kappa, x.e[k].im, lu.e[k].re), fma(-kappa, x.e[k].re, lu.e[k].im));
-    store_mat<T>(lamU + ui, lu);
+    store_link<T>(lamU, ui, lu);
 }
 
 // partials of sum_i a_i b_i (hi arrays of n reals)

@@ -233,13 +233,22 @@ __global__ void __launch_bounds__(128) k_sumsq_delta_batch(BView<T> v, int e_old
             const size_t eb = (size_t)en.tile0 * (D * 8 * kTile);
             const T *eo = sel_e(v, e_old) + eb;
             const T *ew = sel_e(v, e_new) + eb;
-#pragma unroll 8
-            for (int p = 0; p < D * 8; ++p) {
-                const size_t i = tix(site, D * 8, p);
-                const T a = eo[i], b = ew[i];
-                T d = b - a;
-                if (COMP) d += ew[v.elo + i] - eo[v.elo + i];
-                acc = fma(d, a + b, acc);
+#pragma unroll
+            for (int mu = 0; mu < D; ++mu) {
+                const size_t i = tix(site, D * 8, mu * 8);
+                T a[8], b[8], al[8], bl[8];
+                load_efield<T>(eo, i, a);
+                load_efield<T>(ew, i, b);
+                if (COMP) {
+                    load_efield<T>(eo + v.elo, i, al);
+                    load_efield<T>(ew + v.elo, i, bl);
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    T d = b[k] - a[k];
+                    if (COMP) d += bl[k] - al[k];
+                    acc = fma(d, a[k] + b[k], acc);
+                }
             }
         }
         double r[1] = {(double)acc};

@@ -7,7 +7,8 @@
 // of a tile contiguous, plane p of site s at ((s/32)*P + p)*32 + s%32):
 //   links  U : vec2<T>, P = D*9 planes, plane mu*9 + k holds entry k = row*3 + col of U_mu;
 //              with COMP the lo parts follow as a second array of the same shape
-//   efield E : T, P = D*8 planes, plane mu*8 + a holds e^a of E_mu (+ lo array with COMP)
+//   efield E : T, P = D*8 planes, planes mu*8 .. mu*8+7 hold e^a of E_mu, packed per site into
+//              16-byte vectors (efield_off / load_efield) (+ lo array with COMP)
 //   gauss  G : T, P = 9 planes, Hermitian G(x): real diagonal + upper off-diagonal
 // Sites are linearised x_0 fastest as in the reference (src/lattice.rs:909-916), so the
 // +-mu neighbour of a site is +-L^mu with periodic wrap.  Arrays are padded to whole tiles;
@@ -205,19 +206,19 @@ __device__ __forceinline__ void staple_sum(const V2<T> *__restrict__ U, const Ge
         if (nu == mu) continue;
         {
             mat3<T> a, b, t;
-            load_mat<T>(U + tix(xpmu, D * 9, nu * 9), a);
-            load_mat<T>(U + tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), b);
+            load_link<T>(U, tix(xpmu, D * 9, nu * 9), a);
+            load_link<T>(U, tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), b);
             mul_na(a, b, t);
-            load_mat<T>(U + tix(site, D * 9, nu * 9), a);
+            load_link<T>(U, tix(site, D * 9, nu * 9), a);
             mul_na_acc(t, a, sig);
         }
         {
             mat3<T> a, b, w;
             const uint32_t xmnu = bwd(g, site, c[nu], nu);
-            load_mat<T>(U + tix(xmnu, D * 9, mu * 9), a);
-            load_mat<T>(U + tix(bwd(g, xpmu, c[nu], nu), D * 9, nu * 9), b);
+            load_link<T>(U, tix(xmnu, D * 9, mu * 9), a);
+            load_link<T>(U, tix(bwd(g, xpmu, c[nu], nu), D * 9, nu * 9), b);
             mul_nn(a, b, w);
-            load_mat<T>(U + tix(xmnu, D * 9, nu * 9), a);
+            load_link<T>(U, tix(xmnu, D * 9, nu * 9), a);
             mul_an_acc(w, a, sig);
         }
     }
@@ -240,21 +241,21 @@ enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4, MD_EXP = 8, MD_REUNI
 //         With EXP the link moves on the group instead: U' = exp(i drift E) U, the
 //         exponential by su3_exp_i's Cayley-Hamilton recursion; REUNIT then applies
 //         orthonormalize_matrix to the result (in double, from hi + lo).
-// md_update applies the kick (with the staple sum sig) and the drift to link (site, mu).  The
-// link's own values are read through ou / oul (hi / lo link) and oe / oel (hi / lo momenta), each
-// with plane stride kTile: the arrays themselves, or a copy of the block's tiles in shared memory.
+// md_update applies the kick (with the staple sum sig) and the drift to link (site, mu), reading
+// the link and its momenta from Uin / Ein (lo halves at ulo / elo elements further).
 template <int D, typename T, bool COMP, int MODE>
-__device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *ou, const V2<T> *oul, const T *oe,
-                                          const T *oel, V2<T> *__restrict__ Uout, T *Eout, bool copy_e,
-                                          uint32_t site, int mu, T k1, T k2, T drift, size_t ulo, size_t elo) {
+__device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *__restrict__ Uin, const T *Ein,
+                                          V2<T> *__restrict__ Uout, T *Eout, bool copy_e, uint32_t site, int mu,
+                                          T k1, T k2, T drift, size_t ulo, size_t elo) {
     const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
     mat3<T> u;
-    load_mat<T>(ou, u);
+    load_link<T>(Uin, ui, u);
     T e[8], el[8], e_old[8];
+    load_efield<T>(Ein, ei, e);
+    if (COMP) load_efield<T>(Ein + elo, ei, el);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        e[a] = oe[a * kTile];
-        el[a] = COMP ? oel[a * kTile] : T(0);
+        if (!COMP) el[a] = T(0);
         e_old[a] = e[a];
     }
     if (MODE & MD_KICK) {
@@ -266,23 +267,18 @@ __device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *ou, c
             const T k = k1 + k2;
 #pragma unroll
             for (int a = 0; a < 8; a += 2) comp_add2(e[a], e[a + 1], el[a], el[a + 1], k * f[a], k * f[a + 1]);
-        }
+            store_efield<T>(Eout + elo, ei, el);
+        } else {
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            if (COMP) {
-                Eout[elo + ei + a * kTile] = el[a];
-            } else {
+            for (int a = 0; a < 8; ++a) {
                 if (k1 != T(0)) e[a] = fma(k1, f[a], e[a]);
                 e[a] = fma(k2, f[a], e[a]);
             }
-            Eout[ei + a * kTile] = e[a];
         }
+        store_efield<T>(Eout, ei, e);
     } else if (copy_e) {
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            Eout[ei + a * kTile] = e[a];
-            if (COMP) Eout[elo + ei + a * kTile] = el[a];
-        }
+        store_efield<T>(Eout, ei, e);
+        if (COMP) store_efield<T>(Eout + elo, ei, el);
     }
     if (MODE & MD_DRIFT) {
         const T *ed = (MODE & MD_DRIFT_OLD_E) ? e_old : e;
@@ -302,7 +298,7 @@ __device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *ou, c
             for (int k = 0; k < 9; ++k) w.e[k] = cmk(-drift * x.e[k].im, drift * x.e[k].re);
         }
         mat3<T> ul;
-        if (COMP) load_mat<T>(oul, ul);
+        if (COMP) load_link<T>(Uin + ulo, ui, ul);
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
             if (COMP) {
@@ -328,8 +324,8 @@ __device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *ou, c
                 if (COMP) ul.e[k] = cmk(lr, li);
             }
         }
-        if (COMP) store_mat<T>(Uout + ulo + ui, ul);
-        store_mat<T>(Uout + ui, u);
+        if (COMP) store_link<T>(Uout + ulo, ui, ul);
+        store_link<T>(Uout, ui, u);
     }
 }
 // md_link computes link (site, mu): the staple sum first, then the link and momenta of (x, mu)
@@ -345,9 +341,7 @@ __device__ __forceinline__ void md_link(const V2<T> *__restrict__ Uin, V2<T> *__
         site_coords(g, site, c);
         staple_sum<D, T>(Uin, g, site, c, mu, sig);
     }
-    const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
-    md_update<D, T, COMP, MODE>(sig, Uin + ui, Uin + ulo + ui, Ein + ei, Ein + elo + ei, Uout, Eout, Eout != Ein, site,
-                                mu, k1, k2, drift, ulo, elo);
+    md_update<D, T, COMP, MODE>(sig, Uin, Ein, Uout, Eout, Eout != Ein, site, mu, k1, k2, drift, ulo, elo);
 }
 
 template <int D, typename T, bool COMP, int MODE>
@@ -370,8 +364,8 @@ __global__ void k_link_rotate(V2<T> *__restrict__ U, uint32_t V, uint32_t site, 
 #pragma unroll
     for (int b = 0; b < 8; ++b) v[b] = (b == a) ? angle : T(0);
     mat3<T> u, ul, r, w;
-    load_mat<T>(U + ui, u);
-    if (COMP) load_mat<T>(U + ulo + ui, ul);
+    load_link<T>(U, ui, u);
+    if (COMP) load_link<T>(U + ulo, ui, ul);
     su3_exp_i_minus_one<T>(v, r);
     mul_nn(r, u, w);
 #pragma unroll
@@ -384,8 +378,8 @@ __global__ void k_link_rotate(V2<T> *__restrict__ U, uint32_t V, uint32_t site, 
             u.e[k].im += w.e[k].im;
         }
     }
-    store_mat<T>(U + ui, u);
-    if (COMP) store_mat<T>(U + ulo + ui, ul);
+    store_link<T>(U, ui, u);
+    if (COMP) store_link<T>(U + ulo, ui, ul);
 }
 
 // ------------------------------------------------------------------ Gauss law
@@ -440,13 +434,10 @@ __device__ __forceinline__ double gauss_site(const V2<T> *__restrict__ U, const 
             const uint32_t xm = bwd(g, site, c[mu], mu);
             const size_t ex = tix(site, D * 8, mu * 8), emi = tix(xm, D * 8, mu * 8);
             T ex_c[8], em_c[8];
-#pragma unroll
-            for (int a = 0; a < 8; ++a) {
-                ex_c[a] = E[ex + a * kTile];
-                em_c[a] = E[emi + a * kTile];
-            }
+            load_efield<T>(E, ex, ex_c);
+            load_efield<T>(E, emi, em_c);
             mat3<T> u, ex_m, t, w;
-            load_mat<T>(U + tix(xm, D * 9, mu * 9), u);
+            load_link<T>(U, tix(xm, D * 9, mu * 9), u);
             adjoint_to_matrix<T>(ex_c, ex_m);
             adj_mul<T>(em_c, u, t);
             mul_an_herm(u, t, w); // U^dag E U is Hermitian
@@ -510,21 +501,18 @@ __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U,
     mat3<T> u, gx, gp;
     herm_load(G, site, gx);
     herm_load(G, fwd(g, site, c[mu], mu), gp);
-    load_mat<T>(U + tix(site, D * 9, mu * 9), u);
+    load_link<T>(U, tix(site, D * 9, mu * 9), u);
     const size_t ei = tix(site, D * 8, mu * 8);
     T gxc[8], e[8], el[8];
     two_re_tr_generators(gx, gxc);
+    load_efield<T>(E, ei, e);
+    if (COMP) load_efield<T>(E + elo, ei, el);
+    else
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        e[a] = E[ei + a * kTile];
-        el[a] = COMP ? E[elo + ei + a * kTile] : T(0);
-    }
+        for (int a = 0; a < 8; ++a) el[a] = T(0);
     projection_step<T, COMP>(u, gx, gxc, gp, e, el);
-#pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        E[ei + a * kTile] = e[a];
-        if (COMP) E[elo + ei + a * kTile] = el[a];
-    }
+    store_efield<T>(E, ei, e);
+    if (COMP) store_efield<T>(E + elo, ei, el);
 }
 
 // One projection sweep fused with the Gauss law of its result, one thread per site x:
@@ -551,20 +539,17 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
             T e[8], el[8];
             {
                 mat3<T> u, gp, em;
-                load_mat<T>(U + tix(site, D * 9, mu * 9), u);
+                load_link<T>(U, tix(site, D * 9, mu * 9), u);
                 herm_load(Gin, fwd(g, site, c[mu], mu), gp);
                 const size_t ei = tix(site, D * 8, mu * 8);
+                load_efield<T>(Ein, ei, e);
+                if (COMP) load_efield<T>(Ein + elo, ei, el);
+                else
 #pragma unroll
-                for (int a = 0; a < 8; ++a) {
-                    e[a] = Ein[ei + a * kTile];
-                    el[a] = COMP ? Ein[elo + ei + a * kTile] : T(0);
-                }
+                    for (int a = 0; a < 8; ++a) el[a] = T(0);
                 projection_step<T, COMP>(u, gx, gxc, gp, e, el);
-#pragma unroll
-                for (int a = 0; a < 8; ++a) {
-                    Eout[ei + a * kTile] = e[a];
-                    if (COMP) Eout[elo + ei + a * kTile] = el[a];
-                }
+                store_efield<T>(Eout, ei, e);
+                if (COMP) store_efield<T>(Eout + elo, ei, el);
                 adjoint_to_matrix<T>(e, em);
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
@@ -575,16 +560,16 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
             {
                 const uint32_t xm = bwd(g, site, c[mu], mu);
                 mat3<T> w, gm, t, wm;
-                load_mat<T>(U + tix(xm, D * 9, mu * 9), w);
+                load_link<T>(U, tix(xm, D * 9, mu * 9), w);
                 herm_load(Gin, xm, gm);
                 T gmc[8];
                 two_re_tr_generators(gm, gmc);
                 const size_t ei = tix(xm, D * 8, mu * 8);
+                load_efield<T>(Ein, ei, e);
+                if (COMP) load_efield<T>(Ein + elo, ei, el);
+                else
 #pragma unroll
-                for (int a = 0; a < 8; ++a) {
-                    e[a] = Ein[ei + a * kTile];
-                    el[a] = COMP ? Ein[elo + ei + a * kTile] : T(0);
-                }
+                    for (int a = 0; a < 8; ++a) el[a] = T(0);
                 projection_step<T, COMP>(w, gm, gmc, gx, e, el);
                 adj_mul<T>(e, w, t);
                 mul_an_herm(w, t, wm); // U^dag E' U is Hermitian
@@ -635,11 +620,11 @@ __device__ __forceinline__ void plaquette_site(const V2<T> *__restrict__ U, cons
 #pragma unroll
             for (int nu = mu + 1; nu < D; ++nu) {
                 mat3<T> p, q, A, B;
-                load_mat<T>(U + tix(site, D * 9, mu * 9), p);
-                load_mat<T>(U + tix(xpmu, D * 9, nu * 9), q);
+                load_link<T>(U, tix(site, D * 9, mu * 9), p);
+                load_link<T>(U, tix(xpmu, D * 9, nu * 9), q);
                 mul_nn(p, q, A);
-                load_mat<T>(U + tix(site, D * 9, nu * 9), p);
-                load_mat<T>(U + tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), q);
+                load_link<T>(U, tix(site, D * 9, nu * 9), p);
+                load_link<T>(U, tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), q);
                 mul_nn(p, q, B);
                 T re = T(0), im = T(0);
 #pragma unroll
@@ -683,12 +668,12 @@ __device__ __forceinline__ double plaquette_delta_site(const V2<T> *__restrict__
         site_coords(g, site, c);
         auto load_pair = [&](int dir, uint32_t x, mat3<T> &old_hi, mat3<T> &new_hi, mat3<T> &diff) {
             const size_t i = tix(x, D * 9, dir * 9);
-            load_mat<T>(Uo + i, old_hi);
-            load_mat<T>(Un + i, new_hi);
+            load_link<T>(Uo, i, old_hi);
+            load_link<T>(Un, i, new_hi);
             if (COMP) {
                 mat3<T> ol, nl;
-                load_mat<T>(Uo + ulo + i, ol);
-                load_mat<T>(Un + ulo + i, nl);
+                load_link<T>(Uo + ulo, i, ol);
+                load_link<T>(Un + ulo, i, nl);
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
                     diff.e[k].re = (new_hi.e[k].re - old_hi.e[k].re) + (nl.e[k].re - ol.e[k].re);
@@ -734,10 +719,10 @@ __device__ __forceinline__ double plaquette_delta_site(const V2<T> *__restrict__
                 // Evaluated in an order that keeps about four matrices live.
                 mat3<T> q1, t, s1, x_old, x_new, dx, l1;
                 T term = T(0);
-                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
-                load_mat<T>(Un + tix(xpnu, D * 9, mu * 9), t);     // C'
+                load_link<T>(Un, tix(site, D * 9, nu * 9), x_new); // Dd'
+                load_link<T>(Un, tix(xpnu, D * 9, mu * 9), t);     // C'
                 mul_nn(x_new, t, q1);                                  // Q1 = Dd' C'
-                load_mat<T>(Un + tix(xpmu, D * 9, nu * 9), t);     // B'
+                load_link<T>(Un, tix(xpmu, D * 9, nu * 9), t);     // B'
                 mul_na(t, q1, s1);                                     // B' C'^dag Dd'^dag
                 load_pair(mu, site, x_old, x_new, dx);                 // A, A', dA
                 term += re_tr_nn(dx, s1);                              // Tr(dA B' C'^dag Dd'^dag)
@@ -746,7 +731,7 @@ __device__ __forceinline__ double plaquette_delta_site(const V2<T> *__restrict__
                 load_pair(nu, xpmu, x_old, x_new, dx);                 // B, B', dB
                 term += re_tr_nn(dx, t);                               // Tr(A dB C'^dag Dd'^dag)
                 mul_nn(a_old, x_old, l1);                              // L1 = A B
-                load_mat<T>(Un + tix(site, D * 9, nu * 9), x_new); // Dd'
+                load_link<T>(Un, tix(site, D * 9, nu * 9), x_new); // Dd'
                 mul_an(x_new, l1, t);                                  // Dd'^dag A B
                 load_pair(mu, xpnu, x_old, x_new, dx);                 // C, C', dC
                 term += re_tr_na(t, dx);                               // Tr(A B dC^dag Dd'^dag)
@@ -785,7 +770,7 @@ __global__ void __launch_bounds__(128) k_clover_fields(const V2<T> *__restrict__
     if (site >= g.V) return;
     uint32_t c[D];
     site_coords(g, site, c);
-    auto ld = [&](uint32_t x, int dir, mat3<T> &m) { load_mat<T>(U + tix(x, D * 9, dir * 9), m); };
+    auto ld = [&](uint32_t x, int dir, mat3<T> &m) { load_link<T>(U, tix(x, D * 9, dir * 9), m); };
     auto store18 = [](double *dst, const mat3<double> &m) {
 #pragma unroll
         for (int col = 0; col < 3; ++col)
@@ -917,15 +902,15 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
     double r1[3], i1[3], r2[3], i2[3];
 #pragma unroll
     for (int row = 0; row < 3; ++row) {
-        const V2<T> a = U[p0 + (row * 3 + 0) * kTile];
-        const V2<T> b = U[p0 + (row * 3 + 1) * kTile];
+        const V2<T> a = U[p0 + link_off<T>(p0, (row * 3 + 0))];
+        const V2<T> b = U[p0 + link_off<T>(p0, (row * 3 + 1))];
         r1[row] = a.x;
         i1[row] = a.y;
         r2[row] = b.x;
         i2[row] = b.y;
         if (COMP) {
-            const V2<T> al = U[ulo + p0 + (row * 3 + 0) * kTile];
-            const V2<T> bl = U[ulo + p0 + (row * 3 + 1) * kTile];
+            const V2<T> al = U[ulo + p0 + link_off<T>(p0, (row * 3 + 0))];
+            const V2<T> bl = U[ulo + p0 + link_off<T>(p0, (row * 3 + 1))];
             r1[row] += al.x;
             i1[row] += al.y;
             r2[row] += bl.x;
@@ -985,8 +970,8 @@ __global__ void __launch_bounds__(128) k_normalize(V2<T> *__restrict__ U, Geo<D>
             V2<T> h, l;
             split(cols_r[col][row], h.x, l.x);
             split(cols_i[col][row], h.y, l.y);
-            U[p0 + (row * 3 + col) * kTile] = h;
-            if (COMP) U[ulo + p0 + (row * 3 + col) * kTile] = l;
+            U[p0 + link_off<T>(p0, (row * 3 + col))] = h;
+            if (COMP) U[ulo + p0 + link_off<T>(p0, (row * 3 + col))] = l;
         }
 }
 
@@ -1007,7 +992,7 @@ __global__ void __launch_bounds__(128) k_links_from_aos(const double *__restrict
             V2<T> h, l;
             split(src[(col * 3 + row) * 2], h.x, l.x);
             split(src[(col * 3 + row) * 2 + 1], h.y, l.y);
-            const size_t idx = p0 + (row * 3 + col) * kTile;
+            const size_t idx = p0 + link_off<T>(p0, (row * 3 + col));
             U[idx] = h;
             if (COMP) U[ulo + idx] = l;
         }
@@ -1024,7 +1009,7 @@ __global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ 
     for (int col = 0; col < 3; ++col)
 #pragma unroll
         for (int row = 0; row < 3; ++row) {
-            const size_t idx = p0 + (row * 3 + col) * kTile;
+            const size_t idx = p0 + link_off<T>(p0, (row * 3 + col));
             const V2<T> v = U[idx];
             double re = (double)v.x, im = (double)v.y;
             if (COMP) {
@@ -1048,8 +1033,8 @@ __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restric
     for (int a = 0; a < 8; ++a) {
         T h, l;
         split(src[a], h, l);
-        E[ei + a * kTile] = h;
-        if (COMP) E[elo + ei + a * kTile] = l;
+        E[ei + efield_off<T>(ei, a)] = h;
+        if (COMP) E[elo + ei + efield_off<T>(ei, a)] = l;
     }
 }
 template <int D, typename T, bool COMP>
@@ -1062,8 +1047,8 @@ __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, 
     const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        double x = (double)E[ei + a * kTile];
-        if (COMP) x += (double)E[elo + ei + a * kTile];
+        double x = (double)E[ei + efield_off<T>(ei, a)];
+        if (COMP) x += (double)E[elo + ei + efield_off<T>(ei, a)];
         dst[a] = x;
     }
 }
@@ -1092,7 +1077,7 @@ __global__ void __launch_bounds__(128) k_links_identity(V2<T> *__restrict__ U, u
         V2<T> v;
         v.x = (k == 0 || k == 4 || k == 8) ? T(1) : T(0);
         v.y = T(0);
-        U[p0 + k * kTile] = v;
+        U[p0 + link_off<T>(p0, k)] = v;
     }
 }
 
@@ -1169,8 +1154,8 @@ __device__ __forceinline__ void efield_normal_link(T *__restrict__ E, uint32_t s
     const size_t ei = tix(site, D * 8, mu * 8);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        E[ei + a * kTile] = z[a] * sd;
-        if (COMP) E[elo + ei + a * kTile] = T(0);
+        E[ei + efield_off<T>(ei, a)] = z[a] * sd;
+        if (COMP) E[elo + ei + efield_off<T>(ei, a)] = T(0);
     }
 }
 template <int D, typename T, bool COMP>
@@ -1232,11 +1217,11 @@ __global__ void __launch_bounds__(128) k_links_random(V2<T> *__restrict__ U, uin
         split(i1[row], a.y, al.y);
         split(r2[row], b.x, bl.x);
         split(i2[row], b.y, bl.y);
-        U[p0 + (row * 3 + 0) * kTile] = a;
-        U[p0 + (row * 3 + 1) * kTile] = b;
+        U[p0 + link_off<T>(p0, (row * 3 + 0))] = a;
+        U[p0 + link_off<T>(p0, (row * 3 + 1))] = b;
         if (COMP) {
-            U[ulo + p0 + (row * 3 + 0) * kTile] = al;
-            U[ulo + p0 + (row * 3 + 1) * kTile] = bl;
+            U[ulo + p0 + link_off<T>(p0, (row * 3 + 0))] = al;
+            U[ulo + p0 + link_off<T>(p0, (row * 3 + 1))] = bl;
         }
     }
 }

@@ -503,30 +503,91 @@ __device__ __forceinline__ void orthonormalize_d(double (&re)[9], double (&im)[9
 
 // ---- tiled structure-of-arrays storage ----
 // Sites are grouped in tiles of 32 consecutive sites (one warp).  An array of P planes stores
-// plane p of site s at ((s / 32) * P + p) * 32 + s % 32: within a tile all planes of a site
-// are 32 elements apart, so a thread addresses a whole link with one base pointer and
-// constant offsets, and a warp reads each plane of its tile as one contiguous segment.
+// plane p of site s at ((s / 32) * P + p) * 32 + s % 32: a warp reads each plane of its tile as
+// one contiguous segment.
 constexpr int kTile = 32;
 __host__ __device__ __forceinline__ size_t tix(uint32_t site, int nplanes, int plane) {
     return ((size_t)(site >> 5) * nplanes + plane) * kTile + (site & 31);
 }
 __host__ __device__ __forceinline__ uint32_t tiles_of(uint32_t V) { return (V + kTile - 1) / kTile; }
 
-// one link matrix from its 9 complex planes starting at p (entry k at p[k * 32])
-template <typename T> __device__ __forceinline__ void load_mat(const typename vec2_t<T>::type *__restrict__ p, mat3<T> &m) {
+// ---- links and momenta inside a tile ----
+// Links: entry k of the link of (site, mu) is plane mu*9 + k, a float2 / double2 per site: idx =
+// tix(site, P, mu * 9) is entry 0 and entry k lies k * 32 elements further (a warp reads 256 B
+// (FP32) or 512 B (FP64) per entry).  Packing FP32 links into float4 pairs of entries was measured
+// and not kept: the 128-bit destinations raised the MD kernel's register demand past its
+// 96-register budget (spills; 5 % slower at 32^4).
+// Momenta: the 8 planes mu*8 .. mu*8+7 of a tile form a block in which the components of one site
+// are packed into 16-byte vectors -- FP64: components 2q, 2q+1 = double2 plane q (q = 0..3); FP32:
+// components 4q .. 4q+3 = float4 plane q (q = 0, 1) -- so a thread moves its momenta with 4 (FP64)
+// or 2 (FP32) 128-bit accesses and a warp touches 512 contiguous bytes per access.  idx =
+// tix(site, P, mu * 8) is the site's element of plane 0 in the unpacked form; every array base (an
+// allocation, the lo half of a compensated array, an ensemble of a batch, a segment of the
+// adjoint's arena) lies whole tiles from a 256-byte aligned allocation, so idx % 32 is the site's
+// lane and idx - lane the 16-byte aligned block.
+
+// element offset from idx of entry k of a link
+template <typename T> __host__ __device__ __forceinline__ size_t link_off(size_t, int k) { return (size_t)k * kTile; }
+// element offset from idx of momentum component a of a link
+template <typename T> __host__ __device__ __forceinline__ size_t efield_off(size_t idx, int a) {
+    const size_t lane = idx & 31;
+    if constexpr (sizeof(T) == 8) return (size_t)(a >> 1) * (2 * kTile) + lane + (a & 1);
+    else return (size_t)(a >> 2) * (4 * kTile) + 3 * lane + (a & 3);
+}
+
+// one link matrix (read-only path: the arrays read with it are not written by the same launch,
+// except by the reading thread itself after its read)
+template <typename T> __device__ __forceinline__ void load_link(const typename vec2_t<T>::type *__restrict__ U, size_t idx,
+                                                                mat3<T> &m) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-        const typename vec2_t<T>::type v = __ldg(p + k * kTile);
+        const typename vec2_t<T>::type v = __ldg(U + idx + k * kTile);
         m.e[k] = cmk<T>(v.x, v.y);
     }
 }
-template <typename T> __device__ __forceinline__ void store_mat(typename vec2_t<T>::type *__restrict__ p, const mat3<T> &m) {
+template <typename T>
+__device__ __forceinline__ void store_link(typename vec2_t<T>::type *__restrict__ U, size_t idx, const mat3<T> &m) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         typename vec2_t<T>::type v;
         v.x = m.e[k].re;
         v.y = m.e[k].im;
-        p[k * kTile] = v;
+        U[idx + k * kTile] = v;
+    }
+}
+// the 8 momentum components of one link (plain loads: momenta are updated in place)
+template <typename T> __device__ __forceinline__ void load_efield(const T *E, size_t idx, T (&e)[8]) {
+    const size_t lane = idx & 31;
+    if constexpr (sizeof(T) == 8) {
+        const double2 *q = reinterpret_cast<const double2 *>(E + (idx - lane)) + lane;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const double2 v = q[j * kTile];
+            e[2 * j] = v.x;
+            e[2 * j + 1] = v.y;
+        }
+    } else {
+        const float4 *q = reinterpret_cast<const float4 *>(E + (idx - lane)) + lane;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float4 v = q[j * kTile];
+            e[4 * j] = v.x;
+            e[4 * j + 1] = v.y;
+            e[4 * j + 2] = v.z;
+            e[4 * j + 3] = v.w;
+        }
+    }
+}
+template <typename T> __device__ __forceinline__ void store_efield(T *E, size_t idx, const T (&e)[8]) {
+    const size_t lane = idx & 31;
+    if constexpr (sizeof(T) == 8) {
+        double2 *q = reinterpret_cast<double2 *>(E + (idx - lane)) + lane;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) q[j * kTile] = make_double2(e[2 * j], e[2 * j + 1]);
+    } else {
+        float4 *q = reinterpret_cast<float4 *>(E + (idx - lane)) + lane;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) q[j * kTile] = make_float4(e[4 * j], e[4 * j + 1], e[4 * j + 2], e[4 * j + 3]);
     }
 }
 

@@ -201,28 +201,29 @@ __device__ __forceinline__ m2d heat_bath_su2(const m2d &st, double beta, LinkRng
 // the link (site, mu) and its neighbours as double (hi + lo with compensated storage)
 template <typename T, bool COMP>
 __device__ __forceinline__ void load_link_d(const V2<T> *__restrict__ U, size_t ulo, size_t i, mat3<double> &m) {
+    mat3<T> h, l;
+    load_link<T>(U, i, h);
+    if (COMP) load_link<T>(U + ulo, i, l);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-        const V2<T> h = U[i + k * kTile];
-        double re = (double)h.x, im = (double)h.y;
+        double re = (double)h.e[k].re, im = (double)h.e[k].im;
         if (COMP) {
-            const V2<T> l = U[ulo + i + k * kTile];
-            re += (double)l.x;
-            im += (double)l.y;
+            re += (double)l.e[k].re;
+            im += (double)l.e[k].im;
         }
         m.e[k] = cmk(re, im);
     }
 }
 template <typename T, bool COMP>
 __device__ __forceinline__ void store_link_d(V2<T> *__restrict__ U, size_t ulo, size_t i, const mat3<double> &m) {
+    mat3<T> h, l;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-        V2<T> h, l;
-        split(m.e[k].re, h.x, l.x);
-        split(m.e[k].im, h.y, l.y);
-        U[i + k * kTile] = h;
-        if (COMP) U[ulo + i + k * kTile] = l;
+        split(m.e[k].re, h.e[k].re, l.e[k].re);
+        split(m.e[k].im, h.e[k].im, l.e[k].im);
     }
+    store_link<T>(U, i, h);
+    if (COMP) store_link<T>(U + ulo, i, l);
 }
 // the staple of the Monte Carlo methods (src/simulation/monte_carlo/mod.rs:339-362):
 // sum over nu != mu of S_mu,nu(x)^dag + U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)

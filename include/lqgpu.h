@@ -103,6 +103,13 @@ int lq_state_destroy(lq_state *s);
 int lq_state_clone(const lq_state *s, lq_state **out);
 /* Attach a cudaStream_t (passed as void*); NULL selects the legacy default stream. */
 int lq_state_set_stream(lq_state *s, void *cuda_stream);
+/* The Gauss projection's sweep loop (EField::project_to_gauss, src/field.rs:1265-1294) of the
+ * FP32-arithmetic forms runs as one CUDA graph launch whose convergence test is a device kernel
+ * driving a conditional while node (enable = 1, the default), or as host-driven launches with
+ * one host read of the residual per test (enable = 0).  Both give the same sweeps and the same
+ * field; the FP64 form always uses host-driven launches.  A driver that cannot build the graph
+ * turns it off for the state. */
+int lq_state_set_projection_graph(lq_state *s, int enable);
 /* Getters: LatticeCyclic::dim/size, LatticeState::beta, LatticeStateWithEField::t,
  * number_of_points (src/lattice.rs:208-233). is_leap = 1 between sync_leap and leap_sync. */
 int lq_state_info(const lq_state *s, int *dim, int *L, double *size, double *beta, int *precision,

@@ -94,9 +94,7 @@ __device__ __forceinline__ void loop_r(const mat3<T> (&u)[3], const T (&cl)[3][8
 
 template <int D, typename T>
 __device__ __forceinline__ void load_coef(const T *__restrict__ lamE, uint32_t site, int dir, T (&c)[8]) {
-    const size_t ei = tix(site, D * 8, dir * 8);
-#pragma unroll
-    for (int a = 0; a < 8; ++a) c[a] = lamE[ei + efield_off<T>(ei, a)];
+    load_efield<T>(lamE, tix(site, D * 8, dir * 8), c);
 }
 
 // lam_U(m) += coef * i * (sum over the 2(D-1) plaquette loops of m of R)^dag, coef = h c
@@ -176,13 +174,13 @@ __global__ void __launch_bounds__(128) k_adj_drift(const V2<T> *__restrict__ U, 
     load_link<T>(U, ui, u);
     load_link<T>(lamU, ui, lu);
     mat_adj(lu, lua);
-    T f[8], e[8];
+    T f[8], e[8], le[8];
     im_tr_generators_of_product(u, lua, f);
+    load_efield<T>(lamE, ei, le);
+    load_efield<T>(E, ei, e);
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        lamE[ei + efield_off<T>(ei, a)] = fma(-kappa, f[a], lamE[ei + efield_off<T>(ei, a)]);
-        e[a] = E[ei + efield_off<T>(ei, a)];
-    }
+    for (int a = 0; a < 8; ++a) le[a] = fma(-kappa, f[a], le[a]);
+    store_efield<T>(lamE, ei, le);
     adj_mul<T>(e, lu, x); // E lam_U
     // -kappa i x: -i (a + ib) = b - ia
 #pragma unroll

@@ -1029,13 +1029,11 @@ __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restric
     if (site >= V) return;
     const double *src = aos + ((size_t)site * D + mu) * 8;
     const size_t ei = tix(site, D * 8, mu * 8);
+    T h[8], l[8];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        T h, l;
-        split(src[a], h, l);
-        E[ei + efield_off<T>(ei, a)] = h;
-        if (COMP) E[elo + ei + efield_off<T>(ei, a)] = l;
-    }
+    for (int a = 0; a < 8; ++a) split(src[a], h[a], l[a]);
+    store_efield<T>(E, ei, h);
+    if (COMP) store_efield<T>(E + elo, ei, l);
 }
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, double *__restrict__ aos,
@@ -1045,10 +1043,13 @@ __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, 
     if (site >= V) return;
     double *dst = aos + ((size_t)site * D + mu) * 8;
     const size_t ei = tix(site, D * 8, mu * 8);
+    T h[8], l[8];
+    load_efield<T>(E, ei, h);
+    if (COMP) load_efield<T>(E + elo, ei, l);
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        double x = (double)E[ei + efield_off<T>(ei, a)];
-        if (COMP) x += (double)E[elo + ei + efield_off<T>(ei, a)];
+        double x = (double)h[a];
+        if (COMP) x += (double)l[a];
         dst[a] = x;
     }
 }
@@ -1152,11 +1153,14 @@ __device__ __forceinline__ void efield_normal_link(T *__restrict__ E, uint32_t s
         }
     }
     const size_t ei = tix(site, D * 8, mu * 8);
+    T h[8], l[8];
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        E[ei + efield_off<T>(ei, a)] = z[a] * sd;
-        if (COMP) E[elo + ei + efield_off<T>(ei, a)] = T(0);
+        h[a] = z[a] * sd;
+        l[a] = T(0);
     }
+    store_efield<T>(E, ei, h);
+    if (COMP) store_efield<T>(E + elo, ei, l);
 }
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_normal(T *__restrict__ E, uint32_t V, uint2 key, uint32_t ctr_lo,

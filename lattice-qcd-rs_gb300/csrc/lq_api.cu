@@ -60,7 +60,7 @@ void prof_flush(State &s) {
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, p->ev[2 * i], p->ev[2 * i + 1]) == cudaSuccess) {
             p->ms[p->cls[i]] += ms;
-            p->launches[p->cls[i]] += 1;
+            p->launches[p->cls[i]] += p->cnt[i];
         } else {
             (void)cudaGetLastError();
         }
@@ -87,6 +87,7 @@ void prof_end(State &s, int slot, int cls) {
     if (!p || slot < 0) return;
     cudaEventRecord(p->ev[2 * slot + 1], s.stream);
     p->cls[slot] = cls;
+    p->cnt[slot] = 1;
     p->n = slot + 1;
 }
 void prof_free(State &s) {
@@ -116,6 +117,11 @@ void free_state(State *s) {
     if (s->prefetch_done) cudaEventDestroy(s->prefetch_done);
     if (s->prefetch_free) cudaEventDestroy(s->prefetch_free);
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    for (int i = 0; i < s->n_proj; ++i)
+        if (s->proj[i].exec) cudaGraphExecDestroy(s->proj[i].exec);
+    if (s->d_proj) cudaFree(s->d_proj);
+    if (s->cap_main) cudaStreamDestroy(s->cap_main);
+    if (s->cap_body) cudaStreamDestroy(s->cap_body);
     delete static_cast<lq_state *>(s);
 }
 
@@ -194,17 +200,182 @@ int run_symplectic(State &s, int src, double dt, int n, bool e_to_alt, int link_
     return LQ_OK;
 }
 
+// The projection's convergence test on the device, a node of the projection graph: the residual
+// partials are summed exactly as k_finalize<1> sums them (so the value equals the host loop's),
+// the sweeps since the last test are added to ctl[0], and the loop condition is set as the host
+// loop decides: stop on NaN (ctl[1] = LQ_ERR_GAUSS_PROJECTION), at or below the threshold, or
+// when four more sweeps would pass the step limit (ctl[1] = LQ_ERR_NOT_CONVERGED).
+__global__ void __launch_bounds__(1024) k_proj_check(const double *__restrict__ partial, uint32_t n, double threshold,
+                                                     int steps_added, int max_steps, int *ctl,
+                                                     cudaGraphConditionalHandle h) {
+    double v[1] = {0.0};
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) v[0] += partial[k];
+    __shared__ double res[1];
+    lq::block_reduce_store<1>(v, res, 0, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int steps = ctl[0] + steps_added;
+        ctl[0] = steps;
+        const double val = res[0];
+        unsigned int go = 0;
+        if (isnan(val)) ctl[1] = LQ_ERR_GAUSS_PROJECTION;
+        else if (val <= threshold) ctl[1] = LQ_OK;
+        else if (max_steps > 0 && steps + 4 > max_steps) ctl[1] = LQ_ERR_NOT_CONVERGED;
+        else go = 1;
+        cudaGraphSetConditional(h, go);
+    }
+}
+
+double projection_threshold(const State &s) { return eps_of(s) * (double)((uint64_t)s.V * 4 * 8 * 10); }
+
+// Captures the sweep loop of project_gauss for the current link buffer, E/G buffer order and step
+// limit: Gauss law, one sweep, the test, then a while node whose body is four sweeps and the
+// test.  Every run makes 1 + 4k sweeps, so each body leaves E/G in the buffers the first sweep
+// wrote and the baked pointers stay valid for every iteration; the capture itself enqueues (and
+// so swaps the state's E/G pointers) five times, and the order is restored at the end.
+int capture_projection(State &s, int max_steps, cudaGraphExec_t *out) {
+    *out = nullptr;
+    if (!s.d_proj) LQ_CK(cudaMalloc((void **)&s.d_proj, 4 * sizeof(int)));
+    if (!s.cap_main) LQ_CK(cudaStreamCreateWithFlags(&s.cap_main, cudaStreamNonBlocking));
+    if (!s.cap_body) LQ_CK(cudaStreamCreateWithFlags(&s.cap_body, cudaStreamNonBlocking));
+    const void *U = s.U[s.cur];
+    const double threshold = projection_threshold(s);
+    void *E0 = s.E, *E1 = s.E_alt, *G0 = s.G, *G1 = s.G_alt;
+    const cudaStream_t user_stream = s.stream;
+    s.stream = s.cap_main;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s.cap_main, cudaStreamCaptureModeThreadLocal);
+    bool capturing = e == cudaSuccess;
+    cudaGraphConditionalHandle h = 0;
+    uint32_t n = 0;
+    auto sweep = [&]() {
+        cudaError_t r = s.ops->gauss_sweep(s, U, &n);
+        std::swap(s.E, s.E_alt);
+        std::swap(s.G, s.G_alt);
+        return r;
+    };
+    if (e == cudaSuccess) {
+        cudaStreamCaptureStatus st;
+        e = cudaStreamGetCaptureInfo(s.cap_main, &st, nullptr, &g, nullptr, nullptr, nullptr);
+    }
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.d_proj, 0, 4 * sizeof(int), s.stream);
+    if (e == cudaSuccess) e = s.ops->gauss(s, U, &n);
+    if (e == cudaSuccess) e = sweep();
+    if (e == cudaSuccess) {
+        k_proj_check<<<1, 1024, 0, s.stream>>>(s.partial, n, threshold, 1, max_steps, s.d_proj, h);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t *deps = nullptr;
+        const cudaGraphEdgeData *edges = nullptr;
+        size_t ndeps = 0;
+        e = cudaStreamGetCaptureInfo(s.cap_main, &st, nullptr, &g, &deps, &edges, &ndeps);
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, deps, edges, ndeps, &cp);
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(s.cap_main, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e == cudaSuccess) {
+            e = cudaStreamBeginCaptureToGraph(s.cap_body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                s.stream = s.cap_body;
+                for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = sweep();
+                if (e == cudaSuccess) {
+                    k_proj_check<<<1, 1024, 0, s.stream>>>(s.partial, n, threshold, 4, max_steps, s.d_proj, h);
+                    e = cudaGetLastError();
+                }
+                cudaGraph_t body = nullptr;
+                const cudaError_t e2 = cudaStreamEndCapture(s.cap_body, &body);
+                if (e == cudaSuccess) e = e2;
+            }
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    if (capturing) {
+        const cudaError_t e2 = cudaStreamEndCapture(s.cap_main, &graph);
+        if (e == cudaSuccess) e = e2;
+    }
+    s.stream = user_stream;
+    s.E = E0;
+    s.E_alt = E1;
+    s.G = G0;
+    s.G_alt = G1;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(e, "projection graph capture", __LINE__);
+    }
+    return LQ_OK;
+}
+
+// project_gauss through the captured graph: one launch and one read of (sweeps, status)
+int project_gauss_graph(State &s, int max_steps, int *steps_done) {
+    const void *U = s.U[s.cur];
+    cudaGraphExec_t exec = nullptr;
+    for (int i = 0; i < s.n_proj; ++i) {
+        const State::ProjGraph &p = s.proj[i];
+        if (p.U == U && p.E == s.E && p.G == s.G && p.max_steps == max_steps) exec = p.exec;
+    }
+    if (!exec) {
+        if (capture_projection(s, max_steps, &exec) != LQ_OK) {
+            // no graph (a driver without conditional nodes): the host loop from now on
+            s.proj_graph = 0;
+            return -1;
+        }
+        if (s.n_proj == State::kProjGraphs) {
+            // drop the oldest
+            cudaGraphExecDestroy(s.proj[0].exec);
+            for (int i = 1; i < s.n_proj; ++i) s.proj[i - 1] = s.proj[i];
+            --s.n_proj;
+        }
+        s.proj[s.n_proj++] = {U, s.E, s.G, max_steps, exec};
+    }
+    const int slot = prof_begin(s);
+    const cudaError_t e = cudaGraphLaunch(exec, s.stream);
+    prof_end(s, slot, LQ_KERNEL_GAUSS_SWEEP);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch (projection)", __LINE__);
+    // 1 + 4k sweeps: E and G end in the other buffers
+    std::swap(s.E, s.E_alt);
+    std::swap(s.G, s.G_alt);
+    LQ_CK(cudaMemcpyAsync(s.h_out, s.d_proj, 2 * sizeof(int), cudaMemcpyDeviceToHost, s.stream));
+    LQ_CK(cudaStreamSynchronize(s.stream));
+    int ctl[2];
+    memcpy(ctl, s.h_out, sizeof(ctl));
+    // the slot covers the Gauss law, the sweeps and the tests
+    if (s.prof && slot >= 0) s.prof->cnt[slot] = 1 + ctl[0] + (ctl[0] + 3) / 4;
+    prof_flush(s);
+    if (steps_done) *steps_done = ctl[0];
+    if (ctl[1] != LQ_OK) return ctl[1];
+    if (s.comp) {
+        // the sweeps updated the hi parts only: the projected field is hi + 0
+        const size_t half = s.efield_bytes() / 2;
+        LQ_CK(cudaMemsetAsync((char *)s.E + half, 0, half, s.stream));
+    }
+    return LQ_OK;
+}
+
 // EField::project_to_gauss (src/field.rs:1265-1294): one step, then blocks of four steps
 // until the residual of the current field is <= eps * V * 320.  Each sweep also produces
 // G and the residual of its result, so the checks after steps 1, 5, 9, ... read it directly.
 int project_gauss(State &s, int max_steps, int *steps_done) {
-    const double threshold = eps_of(s) * (double)((uint64_t)s.V * 4 * 8 * 10);
-    const void *U = s.U[s.cur];
-    uint32_t n = 0;
-    int steps = 0;
     // FP32 arithmetic: one fused sweep per step (U read once).  FP64: the step and the Gauss
     // law as two kernels, since the sweep's recomputed neighbour updates cost FP64 flops.
     const bool fused = s.precision != LQ_PRECISION_F64;
+    if (fused && s.proj_graph) {
+        const int rc = project_gauss_graph(s, max_steps, steps_done);
+        if (rc != -1) return rc;
+    }
+    const double threshold = projection_threshold(s);
+    const void *U = s.U[s.cur];
+    uint32_t n = 0;
+    int steps = 0;
     LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
     for (;;) {
         if (fused) {
@@ -373,9 +544,16 @@ int lq_state_clone(const lq_state *src, lq_state **out) {
     }
     c->t = src->t;
     c->leap = src->leap;
+    c->proj_graph = src->proj_graph;
     c->hu_valid = src->hu_valid;
     c->hu = src->hu;
     *out = c;
+    return LQ_OK;
+}
+
+int lq_state_set_projection_graph(lq_state *s, int enable) {
+    LQ_CHECK_STATE(s);
+    s->proj_graph = enable ? 1 : 0;
     return LQ_OK;
 }
 

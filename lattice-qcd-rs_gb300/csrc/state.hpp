@@ -17,6 +17,7 @@ constexpr int kProfClasses = 6;
 struct Prof {
     cudaEvent_t ev[2 * kProfPool];
     int cls[kProfPool];
+    int cnt[kProfPool]; // kernels a slot covers (1 for a launch, more for a graph)
     int n = 0;
     long long launches[kProfClasses] = {0, 0, 0, 0, 0, 0};
     double ms[kProfClasses] = {0, 0, 0, 0, 0, 0};
@@ -53,6 +54,23 @@ struct State {
     cudaEvent_t prefetch_done = nullptr; // the copy has landed
     cudaEvent_t prefetch_free = nullptr; // the last prefetched field has been consumed
     int prefetch_pending = 0;
+
+    // the Gauss projection's sweep loop as a CUDA graph whose while node the device-side check
+    // drives (lq_state_set_projection_graph; FP32 arithmetic forms): one instantiation per
+    // (link buffer, E/G buffer order, step limit) met, built on first use
+    struct ProjGraph {
+        const void *U;
+        const void *E;
+        const void *G;
+        int max_steps;
+        cudaGraphExec_t exec;
+    };
+    static constexpr int kProjGraphs = 8;
+    int proj_graph = 1;
+    ProjGraph proj[kProjGraphs] = {};
+    int n_proj = 0;
+    int *d_proj = nullptr; // device: sweeps done, status
+    cudaStream_t cap_main = nullptr, cap_body = nullptr;
 
     long long t = 0;
     int leap = 0;

@@ -47,6 +47,7 @@ SIGNATURES = {
     "lq_state_destroy": (_i32, [_vp]),
     "lq_state_clone": (_i32, [_vp, ctypes.POINTER(_vp)]),
     "lq_state_set_stream": (_i32, [_vp, _vp]),
+    "lq_state_set_projection_graph": (_i32, [_vp, _i32]),
     "lq_state_info": (_i32, [_vp, _ip, _ip, _dp, _dp, _ip, _llp, _llp, _ip]),
     "lq_state_set_beta": (_i32, [_vp, _f64]),
     "lq_state_set_link_update": (_i32, [_vp, _i32]),
@@ -188,6 +189,10 @@ class State:
 
     def set_stream(self, stream_ptr):
         _check(load().lq_state_set_stream(self._h, _vp(stream_ptr)), "lq_state_set_stream")
+
+    def set_projection_graph(self, enable):
+        """Gauss projection as one graph launch (True, the default) or host-driven launches."""
+        _check(load().lq_state_set_projection_graph(self._h, 1 if enable else 0), "lq_state_set_projection_graph")
 
     def info(self):
         d, L, pr, leap = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

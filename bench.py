@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--projection", default="graph", choices=["graph", "host"],
+                    help="Gauss projection loop of the headline state: one graph launch with a device-side test "
+                         "(default) or host-driven launches (profilers do not see kernels inside graphs with "
+                         "conditional nodes)")
     ap.add_argument("--batch-traj", type=int, default=10,
                     help="timed trajectories of the batched-ensembles leg (0: skip it)")
     return ap.parse_args()
@@ -343,6 +347,7 @@ def run_ours(args):
     # ---- headline precision
     s = lqgpu.State(dim, L, size, beta, prec)
     s.set_stream(stream.cuda_stream)
+    s.set_projection_graph(args.projection == "graph")
     s.set_links_random(1 + rank)
     s.profile_enable(True)
     ms, wall, prof, res, clocks = timed_trajectories(s, args.warmup, args.steps, 77 + rank, sample_clocks=True)
@@ -473,6 +478,7 @@ def run_ours(args):
                                    "random_su3 start, device momenta N(0,0.5/beta) + Gauss projection"
                                    % (dim, L, dim, beta, nmd, dt, size),
                        "precision": args.precision, "parallelism": "replicas" if world > 1 else "single GPU",
+                       "projection_loop": args.projection,
                        "l2": "inputs larger than L2 (links %.0f MB)" % (n_links * 18 * real_bytes / 1e6)},
             "roofline": {"bound": "hbm", "kernel": "k_md (fused force + kick + drift)", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,

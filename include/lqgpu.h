@@ -108,7 +108,8 @@ int lq_state_set_stream(lq_state *s, void *cuda_stream);
  * driving a conditional while node (enable = 1, the default), or as host-driven launches with
  * one host read of the residual per test (enable = 0).  Both give the same sweeps and the same
  * field; the FP64 form always uses host-driven launches.  A driver that cannot build the graph
- * turns it off for the state. */
+ * turns it off for the state.  Without a step limit (max_steps <= 0) the graph's device-side loop
+ * still stops after 2^20 sweeps with LQ_ERR_NOT_CONVERGED. */
 int lq_state_set_projection_graph(lq_state *s, int enable);
 /* Getters: LatticeCyclic::dim/size, LatticeState::beta, LatticeStateWithEField::t,
  * number_of_points (src/lattice.rs:208-233). is_leap = 1 between sync_leap and leap_sync. */

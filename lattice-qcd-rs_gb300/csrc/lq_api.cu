@@ -315,8 +315,13 @@ int capture_projection(State &s, int max_steps, cudaGraphExec_t *out) {
     return LQ_OK;
 }
 
+// A step limit for the graph's device-side loop when the caller sets none (max_steps <= 0): the
+// loop always ends (after 2^20 sweeps, several minutes at 32^4, with LQ_ERR_NOT_CONVERGED).
+constexpr int kProjGraphMaxSweeps = 1 << 20;
+
 // project_gauss through the captured graph: one launch and one read of (sweeps, status)
 int project_gauss_graph(State &s, int max_steps, int *steps_done) {
+    if (max_steps <= 0) max_steps = kProjGraphMaxSweeps;
     const void *U = s.U[s.cur];
     cudaGraphExec_t exec = nullptr;
     for (int i = 0; i < s.n_proj; ++i) {

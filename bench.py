@@ -209,9 +209,9 @@ def run_reference(args):
 
 # ------------------------------------------------------------------ GPU arm
 # DRAM bytes (read + write) per link of one k_md kick+drift launch, from one ncu capture of the
-# mixed kernel at 28^4 (995.1 MB for 2,458,624 links); traffic scales with the links of a launch,
+# mixed kernel at 28^4 (994.9 MB for 2,458,624 links); traffic scales with the links of a launch,
 # so the full-size value is this times the links.
-NCU_MD_TRAFFIC_PER_LINK = {"mixed": 995.1e6 / 2458624}
+NCU_MD_TRAFFIC_PER_LINK = {"mixed": 994.9e6 / 2458624}
 
 
 def algorithmic_md_bytes(n_links, md_steps, real_bytes):

@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--size", type=float, default=1000.0)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "f32", "f64"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed FP64 trajectories for the comparison leg")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-sample-L", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -388,8 +388,10 @@ def run_ours(args):
             p, h0, h1 = s.hmc_propose(dt, nmd)
             s.hmc_decide(p >= 1.0 or float(uni.uniform()) < p)
             plaq = s.average_trace_plaquette()
-            # residual reads of the projection (one double per check) + 8 doubles (proposal) + 3 (plaquette)
-            d2h += 8 * ((steps - 1) // 4 + 1) + 8 * 8 + 8 * 3
+            # the projection's reads (graph: sweeps and status, 2 ints; host loop: one double per test)
+            # + 8 doubles (proposal) + 3 (plaquette)
+            proj_d2h = 8 if args.projection == "graph" else 8 * ((steps - 1) // 4 + 1)
+            d2h += proj_d2h + 8 * 8 + 8 * 3
         ev1.record(stream)
         torch.cuda.synchronize()
         e2e_ms = max_over_ranks(ev0.elapsed_time(ev1))

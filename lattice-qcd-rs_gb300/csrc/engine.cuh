@@ -158,6 +158,7 @@ template <int D, typename T, bool COMP> struct Engine {
     static cudaError_t finalize(State &s, int nv, uint32_t n, int offset) {
         switch (nv) {
         case 1: k_finalize<1><<<1, 1024, 0, s.stream>>>(s.partial, n, s.d_out + offset); break;
+        case 2: k_finalize<2><<<1, 1024, 0, s.stream>>>(s.partial, n, s.d_out + offset); break;
         case 3: k_finalize<3><<<1, 1024, 0, s.stream>>>(s.partial, n, s.d_out + offset); break;
         default: return cudaErrorInvalidValue;
         }

@@ -878,15 +878,23 @@ __global__ void __launch_bounds__(256) k_sum_squares(const T *__restrict__ x, si
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(256) k_sum_squares_delta(const T *__restrict__ eo, const T *__restrict__ en, size_t n,
                                                            double *__restrict__ partial) {
-    T acc = T(0);
+    // row 0: sum (e' - e)(e' + e); row 1: sum e^2 of eo, element for element and in the order
+    // of k_sum_squares on the same launch shape, so it equals k_sum_squares(eo) bitwise
+    T acc = T(0), sq = T(0);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const T a = eo[i], b = en[i];
         T d = b - a;
-        if (COMP) d += en[n + i] - eo[n + i];
+        if (COMP) {
+            const T al = eo[n + i];
+            d += en[n + i] - al;
+            sq = fma(a, a, fma(T(2) * a, al, sq));
+        } else {
+            sq = fma(a, a, sq);
+        }
         acc = fma(d, a + b, acc);
     }
-    double v[1] = {(double)acc};
-    block_reduce_store<1>(v, partial, blockIdx.x, gridDim.x);
+    double v[2] = {(double)acc, (double)sq};
+    block_reduce_store<2>(v, partial, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ reprojection

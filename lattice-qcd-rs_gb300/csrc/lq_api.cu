@@ -1151,13 +1151,17 @@ int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_
     State &st = *s;
     st.has_pending = 0;
     int rc = LQ_OK;
-    // H of the start state: d_out[0..2] plaquette sums (unless cached), d_out[3] sum e^2
+    // H of the start state: d_out[0..2] plaquette sums (unless cached); sum e^2 in d_out[3] (FP64,
+    // here) or d_out[6] (FP32 arithmetic, from the difference kernel after the MD, which reads the
+    // start momenta anyway: they stay in st.E)
     if (!st.hu_valid) {
         rc = plaquette_sums(st, st.U[st.cur], 0);
         if (rc) return rc;
     }
-    rc = efield_sumsq(st, 3);
-    if (rc) return rc;
+    if (st.precision == LQ_PRECISION_F64) {
+        rc = efield_sumsq(st, 3);
+        if (rc) return rc;
+    }
     int fin = -1;
     rc = run_symplectic(st, st.cur, dt, n_steps, true, st.link_update, &fin); // start momenta stay in st.E
     if (rc) return rc;
@@ -1176,17 +1180,18 @@ int lq_hmc_propose(lq_state *s, double dt, int n_steps, double *prob, double *h_
         he_new = st.h_out[7] / 2.0 * st.beta;
     } else {
         // FP32 arithmetic: Delta H from the difference kernels (no cancellation between two
-        // large sums); d_out[4] = sum Re Tr[P' - P], d_out[5] = sum (e' - e)(e' + e)
+        // large sums); d_out[4] = sum Re Tr[P' - P], d_out[5] = sum (e' - e)(e' + e),
+        // d_out[6] = sum e^2 of the start momenta
         uint32_t n = 0;
         LQ_LAUNCH(st, LQ_KERNEL_PLAQUETTE, st.ops->plaquette_delta(st, st.U[st.cur], st.U[fin], &n));
         LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->finalize(st, 1, n, 4));
         LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->efield_sumsq_delta(st, st.E, st.E_alt, &n));
-        LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->finalize(st, 1, n, 5));
-        rc = fetch_out(st, 6);
+        LQ_LAUNCH(st, LQ_KERNEL_REDUCE, st.ops->finalize(st, 2, n, 5));
+        rc = fetch_out(st, 7);
         if (rc) return rc;
         std::swap(st.E, st.E_alt);
         hu_old = st.hu_valid ? st.hu : st.h_out[0] * st.beta;
-        he_old = st.h_out[3] / 2.0 * st.beta;
+        he_old = st.h_out[6] / 2.0 * st.beta;
         hu_new = hu_old - st.h_out[4] / 3.0 * st.beta;
         he_new = he_old + st.h_out[5] / 2.0 * st.beta;
     }

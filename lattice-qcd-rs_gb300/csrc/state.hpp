@@ -123,7 +123,7 @@ struct Ops {
     // partials of sum Re Tr[P(Unew) - P(Uold)]
     cudaError_t (*plaquette_delta)(State &s, const void *Uold, const void *Unew, uint32_t *n_partials);
     cudaError_t (*efield_sumsq)(State &s, const void *E, uint32_t *n_partials);
-    // partials of sum (e_new - e_old)(e_new + e_old)
+    // partials (2 rows) of sum (e_new - e_old)(e_new + e_old) and of sum e_old^2 (as efield_sumsq)
     cudaError_t (*efield_sumsq_delta)(State &s, const void *Eold, const void *Enew, uint32_t *n_partials);
     cudaError_t (*normalize)(State &s, void *U);
     // finalize NV rows of n partials into d_out[offset..]

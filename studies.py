@@ -26,7 +26,9 @@ adjoint   : d<plaq>/dbeta through a 50-step leap-frog at 48^4 by the checkpointe
 distribution: HMC and checkerboard Metropolis on the same lattice and beta give the same average
             plaquette within statistical errors (both sample the Wilson measure).
 
-usage: python studies.py precision [--traj N] [--size L] | scale [--traj K] [--size L] | batch [--traj N] | adjoint [--L 48]
+tour      : every kernel once (for a per-kernel ncu launch list with DRAM bytes).
+
+usage: python studies.py precision [--traj N] [--size L] | scale [--traj K] [--size L] | tour [--L 24] | batch [--traj N] | adjoint [--L 48]
        | distribution [--therm N --meas M]
 """
 import argparse
@@ -426,9 +428,86 @@ def distribution_study(args):
     return out
 
 
+def tour_study(args):
+    """Every kernel of the library launched at least once, for a per-kernel profile (a launch list with
+    DRAM bytes under ncu): D = 4 states at L^4 (default 24^4, links above L2 in every form) in FP64,
+    mixed and f32 -- conversions, momentum draws, Gauss law, projection (host-driven loop, so that
+    profilers see its kernels), the MD modes and the exponential update, the HMC proposal, the action and
+    its backward, a link rotation, normalisation, clover fields, Metropolis and heat-bath sweeps and the
+    trajectory adjoint -- a D = 3 and a D = 2 trajectory, the allocation-free plaquette sums, and a
+    batch of 8 uneven ensembles run eagerly."""
+    import ctypes
+
+    import torch
+
+    L, dt = args.L if args.L != 32 else 24, 0.005
+    done = []
+    for prec in (lqgpu.PRECISION_F64, lqgpu.PRECISION_MIXED, lqgpu.PRECISION_F32):
+        with lqgpu.State(4, L, 1000.0, 2.0, prec) as s:
+            s.set_projection_graph(False)
+            s.set_links_cold()
+            s.set_links_random(1)
+            links = s.link_matrix()
+            s.set_link_matrix(links)
+            s.set_e_field_normal(2, 0, 0.25)
+            e = s.e_field()
+            s.set_e_field(e)
+            s.gauss()
+            s.gauss_sum_div()
+            s.project_to_gauss()
+            s.hamiltonian_links()
+            s.hamiltonian_efield()
+            s.average_trace_plaquette()
+            for mode in (lqgpu.SYNC_SYNC, lqgpu.SYNC_LEAP, lqgpu.LEAP_LEAP, lqgpu.LEAP_SYNC):
+                s.integrate(mode, dt, 1)
+            s.integrate(lqgpu.SYMPLECTIC, dt, 2)
+            s.integrate(lqgpu.SYMPLECTIC_EXP, dt, 1)
+            s.integrate(lqgpu.SYMPLECTIC_EXP_REUNITARIZE, dt, 1)
+            s.normalize_link_matrices()
+            s.hmc_trajectory(dt, 3, 5, 0, 0.5)
+            s.wilson_action()
+            s.wilson_action_backward()
+            s.link_rotate(7, 3, 1e-3)
+            s.field_strength()
+            s.magnetic_field()
+            s.metropolis_sweep(1, 0.1, 3, 0)
+            s.heat_bath_sweep(3, 1)
+            s.leapfrog_adjoint(dt, 4)
+        done.append(PREC_NAMES[prec])
+    for dim, Ld in ((3, 64), (2, 512)):
+        with lqgpu.State(dim, Ld, 1000.0, 2.0, lqgpu.PRECISION_MIXED) as s:
+            s.set_projection_graph(False)
+            s.set_links_random(1)
+            s.hmc_trajectory(dt, 3, 5, 0, 0.5)
+        done.append("mixed D=%d" % dim)
+    lib = lqgpu.load()
+    dev = torch.device("cuda:0")
+    with lqgpu.State(4, L, 1000.0, 2.0, lqgpu.PRECISION_F64) as s:
+        s.set_links_random(3)
+        d_links = torch.from_numpy(s.link_matrix()).to(dev)
+    d_out = torch.zeros(3, dtype=torch.float64, device=dev)
+    rc = lib.lq_plaquette_sums_noalloc(4, L, ctypes.c_void_p(d_links.data_ptr()), ctypes.c_void_p(d_out.data_ptr()),
+                                       ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    torch.cuda.synchronize(dev)
+    if rc != lqgpu.LQ_OK:
+        raise lqgpu.LqError(rc, "lq_plaquette_sums_noalloc")
+    done.append("noalloc plaquette sums")
+    Ls = [8, 10, 12, 16, 8, 10, 12, 16]
+    with lqgpu.Batch(4, Ls, [1000.0] * len(Ls), np.linspace(1.0, 3.0, len(Ls)), lqgpu.PRECISION_MIXED) as b:
+        b.set_links_random(3)
+        b.set_seed(3, 0)
+        b.hmc_run(0.01, 3, 1, graph=False, measure_plaquette=True)
+        b.normalize_link_matrices()
+        b.average_trace_plaquette()
+    done.append("batch (eager)")
+    out = {"study": "tour", "L": L, "done": done}
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "scale", "batch", "adjoint", "distribution"])
+    ap.add_argument("study", choices=["precision", "scale", "batch", "adjoint", "distribution", "tour"])
     ap.add_argument("--traj", type=int, default=None)
     ap.add_argument("--L", type=int, default=32)
     ap.add_argument("--betas", type=float, nargs="*", default=[0.5, 1.0, 2.0, 4.0])
@@ -453,6 +532,8 @@ def main():
         res = batch_study(args)
     elif args.study == "distribution":
         res = distribution_study(args)
+    elif args.study == "tour":
+        res = tour_study(args)
     else:
         if args.L == 32:
             args.L = 48

@@ -26,9 +26,9 @@ adjoint   : d<plaq>/dbeta through a 50-step leap-frog at 48^4 by the checkpointe
 distribution: HMC and checkerboard Metropolis on the same lattice and beta give the same average
             plaquette within statistical errors (both sample the Wilson measure).
 
-tour      : every kernel once (for a per-kernel ncu launch list with DRAM bytes).
+tour      : every kernel once at 32^4 (for a per-kernel ncu launch list with DRAM bytes).
 
-usage: python studies.py precision [--traj N] [--size L] | scale [--traj K] [--size L] | tour [--L 24] | batch [--traj N] | adjoint [--L 48]
+usage: python studies.py precision [--traj N] [--size L] | scale [--traj K] [--size L] | tour [--L 32] | batch [--traj N] | adjoint [--L 48]
        | distribution [--therm N --meas M]
 """
 import argparse
@@ -430,17 +430,17 @@ def distribution_study(args):
 
 def tour_study(args):
     """Every kernel of the library launched at least once, for a per-kernel profile (a launch list with
-    DRAM bytes under ncu): D = 4 states at L^4 (default 24^4, links above L2 in every form) in FP64,
+    DRAM bytes under ncu): D = 4 states at L^4 (default 32^4: links and momenta above L2) in FP64,
     mixed and f32 -- conversions, momentum draws, Gauss law, projection (host-driven loop, so that
     profilers see its kernels), the MD modes and the exponential update, the HMC proposal, the action and
     its backward, a link rotation, normalisation, clover fields, Metropolis and heat-bath sweeps and the
-    trajectory adjoint -- a D = 3 and a D = 2 trajectory, the allocation-free plaquette sums, and a
-    batch of 8 uneven ensembles run eagerly."""
+    trajectory adjoint -- a D = 3 (128^3) and a D = 2 (2048^2) trajectory, the allocation-free plaquette
+    sums, and a batch of 8 uneven ensembles (L 16 .. 28, 9.4 M links) run eagerly."""
     import ctypes
 
     import torch
 
-    L, dt = args.L if args.L != 32 else 24, 0.005
+    L, dt = args.L, 0.005
     done = []
     for prec in (lqgpu.PRECISION_F64, lqgpu.PRECISION_MIXED, lqgpu.PRECISION_F32):
         with lqgpu.State(4, L, 1000.0, 2.0, prec) as s:
@@ -474,7 +474,7 @@ def tour_study(args):
             s.heat_bath_sweep(3, 1)
             s.leapfrog_adjoint(dt, 4)
         done.append(PREC_NAMES[prec])
-    for dim, Ld in ((3, 64), (2, 512)):
+    for dim, Ld in ((3, 128), (2, 2048)):
         with lqgpu.State(dim, Ld, 1000.0, 2.0, lqgpu.PRECISION_MIXED) as s:
             s.set_projection_graph(False)
             s.set_links_random(1)
@@ -492,7 +492,7 @@ def tour_study(args):
     if rc != lqgpu.LQ_OK:
         raise lqgpu.LqError(rc, "lq_plaquette_sums_noalloc")
     done.append("noalloc plaquette sums")
-    Ls = [8, 10, 12, 16, 8, 10, 12, 16]
+    Ls = [16, 20, 24, 28, 16, 20, 24, 28]
     with lqgpu.Batch(4, Ls, [1000.0] * len(Ls), np.linspace(1.0, 3.0, len(Ls)), lqgpu.PRECISION_MIXED) as b:
         b.set_links_random(3)
         b.set_seed(3, 0)

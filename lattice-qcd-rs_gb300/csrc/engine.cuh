@@ -12,6 +12,8 @@ namespace lq {
 template <int D, typename T, bool COMP> struct Engine {
     static Geo<D> geo(const State &s) { return make_geo<D>(s.V, (uint32_t)s.L); }
     static dim3 link_grid(const State &s, int threads) { return dim3((s.V + threads - 1) / threads, D, 1); }
+    // one thread per link, directions fastest
+    static uint32_t link_blocks(const State &s, int threads) { return (uint32_t)(((uint64_t)s.V * D + threads - 1) / threads); }
     // distance in elements from the hi array to the lo array of compensated links / E-field
     static size_t ulo(const State &s) { return (size_t)tiles_of(s.V) * D * 9 * kTile; }
     static size_t elo(const State &s) { return (size_t)tiles_of(s.V) * D * 8 * kTile; }
@@ -40,11 +42,11 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
     static cudaError_t efield_from_aos(State &s, const double *d_aos) {
-        k_efield_from_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V, elo(s));
+        k_efield_from_aos<D, T, COMP><<<link_blocks(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V, elo(s));
         return cudaGetLastError();
     }
     static cudaError_t efield_to_aos(State &s, const void *E, double *d_aos) {
-        k_efield_to_aos<D, T, COMP><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)E, d_aos, s.V, elo(s));
+        k_efield_to_aos<D, T, COMP><<<link_blocks(s, 128), 128, 0, s.stream>>>((const T *)E, d_aos, s.V, elo(s));
         return cudaGetLastError();
     }
     // out <- scale * Im Tr(T^a U_mu(x) Sigma_mu(x)) on every link (out zeroed by the caller)
@@ -193,7 +195,7 @@ template <int D, typename T, bool COMP> struct Engine {
         return cudaGetLastError();
     }
     static cudaError_t cot_efield_to_aos(State &s, const void *lamE, double *d_aos) {
-        k_efield_to_aos<D, T, false><<<link_grid(s, 128), 128, 0, s.stream>>>((const T *)lamE, d_aos, s.V, 0);
+        k_efield_to_aos<D, T, false><<<link_blocks(s, 128), 128, 0, s.stream>>>((const T *)lamE, d_aos, s.V, 0);
         return cudaGetLastError();
     }
 

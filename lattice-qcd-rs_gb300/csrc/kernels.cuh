@@ -1032,33 +1032,44 @@ __global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ 
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restrict__ aos, T *__restrict__ E,
                                                          uint32_t V, size_t elo) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    const int mu = blockIdx.y;
+    // one thread per link, the D directions of a site on consecutive threads: a warp reads 2 KB of the
+    // reference layout contiguously (128-bit loads)
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t site = t / D;
+    const int mu = (int)(t % D);
     if (site >= V) return;
-    const double *src = aos + ((size_t)site * D + mu) * 8;
-    const size_t ei = tix(site, D * 8, mu * 8);
+    const double2 *src = reinterpret_cast<const double2 *>(aos + (size_t)t * 8);
     T h[8], l[8];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) split(src[a], h[a], l[a]);
+    for (int j = 0; j < 4; ++j) {
+        const double2 v = __ldg(src + j);
+        split(v.x, h[2 * j], l[2 * j]);
+        split(v.y, h[2 * j + 1], l[2 * j + 1]);
+    }
+    const size_t ei = tix(site, D * 8, mu * 8);
     store_efield<T>(E, ei, h);
     if (COMP) store_efield<T>(E + elo, ei, l);
 }
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_efield_to_aos(const T *__restrict__ E, double *__restrict__ aos,
                                                        uint32_t V, size_t elo) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
-    const int mu = blockIdx.y;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t site = t / D;
+    const int mu = (int)(t % D);
     if (site >= V) return;
-    double *dst = aos + ((size_t)site * D + mu) * 8;
     const size_t ei = tix(site, D * 8, mu * 8);
     T h[8], l[8];
     load_efield<T>(E, ei, h);
     if (COMP) load_efield<T>(E + elo, ei, l);
+    double2 *dst = reinterpret_cast<double2 *>(aos + (size_t)t * 8);
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        double x = (double)h[a];
-        if (COMP) x += (double)l[a];
-        dst[a] = x;
+    for (int j = 0; j < 4; ++j) {
+        double x0 = (double)h[2 * j], x1 = (double)h[2 * j + 1];
+        if (COMP) {
+            x0 += (double)l[2 * j];
+            x1 += (double)l[2 * j + 1];
+        }
+        dst[j] = make_double2(x0, x1);
     }
 }
 // G(x) as its 8 su(3) coefficients g^a = 2 Re Tr(T^a G(x))

@@ -75,14 +75,15 @@ __device__ __forceinline__ uint32_t bwd(const Geo<D> &g, uint32_t site, uint32_t
 template <typename T> using V2 = typename vec2_t<T>::type;
 
 // Minimum resident blocks per SM requested from the register allocator for the FP32 forms
-// of the MD kernel and the projection sweep (1: no request; 5 measured best on GB300 at
-// 32^4, about 96 registers).  The FP64 forms keep the
-// allocator's choice: their working set needs about twice the registers.
+// of the MD kernel and the projection sweep (1: no request).  Measured on GB300 at 32^4: the MD
+// kernel is best at 5 (96 registers; 4: +5 %, 6: +1 %), the sweep at 4 (128 registers, no spills;
+// 5: +1 %, 6: +3 %).  The FP64 forms keep the allocator's choice: their working set needs about
+// twice the registers.
 #ifndef LQ_MD_MIN_BLOCKS
 #define LQ_MD_MIN_BLOCKS 5
 #endif
 #ifndef LQ_SWEEP_MIN_BLOCKS
-#define LQ_SWEEP_MIN_BLOCKS 5
+#define LQ_SWEEP_MIN_BLOCKS 4
 #endif
 
 template <typename T> struct MinBlocks {

@@ -57,7 +57,8 @@ struct State {
 
     // the Gauss projection's sweep loop as a CUDA graph whose while node the device-side check
     // drives (lq_state_set_projection_graph; FP32 arithmetic forms): one instantiation per
-    // (link buffer, E/G buffer order, step limit) met, built on first use
+    // (link buffer, E buffer order, G buffer order, step limit) met, built on first use; 12 entries
+    // hold every combination of the 3 link buffers and 2 x 2 buffer orders (an HMC loop meets 6)
     struct ProjGraph {
         const void *U;
         const void *E;
@@ -65,7 +66,7 @@ struct State {
         int max_steps;
         cudaGraphExec_t exec;
     };
-    static constexpr int kProjGraphs = 8;
+    static constexpr int kProjGraphs = 12;
     int proj_graph = 1;
     ProjGraph proj[kProjGraphs] = {};
     int n_proj = 0;

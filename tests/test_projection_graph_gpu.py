@@ -89,6 +89,20 @@ def test_projection_graph_errors(lqgpu_mod, precision):
         assert np.array_equal(a.e_field(), b.e_field())
 
 
+@pytest.mark.parametrize("precision", [1, 2])
+def test_projection_graph_without_step_limit(lqgpu_mod, precision):
+    """max_steps <= 0: the host loop has no limit, the graph its own bound; a field that converges
+    gives the same sweeps and field either way."""
+    G = lqgpu_mod
+    a, b = pair(G, precision, seed=4)
+    e_raw = np.random.default_rng(9).normal(0.0, 0.5 / BETA, size=(L ** DIM, DIM, 8))
+    with a, b:
+        for s in (a, b):
+            s.set_e_field(e_raw)
+        assert a.project_to_gauss(max_steps=0) == b.project_to_gauss(max_steps=0)
+        assert np.array_equal(a.e_field(), b.e_field())
+
+
 def test_projection_graph_profile_counts(lqgpu_mod):
     """The graph's profile slot counts the Gauss law, every sweep and every test."""
     G = lqgpu_mod

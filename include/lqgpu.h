@@ -244,7 +244,10 @@ int lq_leapfrog_adjoint(lq_state *s, double dt, int n_steps, int checkpoint_ever
  * :573-613), split as the reference splits it:
  *   refresh     : new_random_e_state (src/simulation/state.rs:1093-1108) -- draw E ~ N(0, 0.5/beta)
  *                 then project_to_gauss; lq_hmc_refresh draws on the device, lq_hmc_refresh_upload
- *                 takes the drawn field from the host (test mode).
+ *                 takes the drawn field from the host (test mode).  The projection works on the
+ *                 hi parts of a compensated (mixed) field and clears the lo parts when it
+ *                 finishes, so the field enters with lo = 0 (after a failed projection the
+ *                 field is its hi parts).
  *   propose     : simulate_symplectic_n_auto(dt, n) + probability_of_replacement
  *                 prob = clamp(exp(H_old - H_new), 0, 1); the start state is kept.
  *   decide      : Bernoulli(prob) -- accept = 1 keeps the proposal, 0 restores the start state

@@ -45,6 +45,11 @@ template <int D, typename T, bool COMP> struct Engine {
         k_efield_from_aos<D, T, COMP><<<link_blocks(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V, elo(s));
         return cudaGetLastError();
     }
+    static cudaError_t efield_hi_from_aos(State &s, const double *d_aos) {
+        k_efield_from_aos<D, T, COMP, false>
+            <<<link_blocks(s, 128), 128, 0, s.stream>>>(d_aos, (T *)s.E, s.V, elo(s));
+        return cudaGetLastError();
+    }
     static cudaError_t efield_to_aos(State &s, const void *E, double *d_aos) {
         k_efield_to_aos<D, T, COMP><<<link_blocks(s, 128), 128, 0, s.stream>>>((const T *)E, d_aos, s.V, elo(s));
         return cudaGetLastError();
@@ -229,7 +234,7 @@ template <int D, typename T, bool COMP> struct Engine {
                                 gauss_step,     gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
                                 normalize,      finalize,       force,         link_rotate,
                                 adj_init,       adj_kick,       adj_drift,     dot,
-                                cot_links_to_aos, cot_efield_to_aos, clover_fields, mc_sweep};
+                                cot_links_to_aos, cot_efield_to_aos, clover_fields, mc_sweep, efield_hi_from_aos};
         return &ops;
     }
 };

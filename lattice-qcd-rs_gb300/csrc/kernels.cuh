@@ -1030,7 +1030,10 @@ __global__ void __launch_bounds__(128) k_links_to_aos(const V2<T> *__restrict__ 
             dst[(col * 3 + row) * 2 + 1] = im;
         }
 }
-template <int D, typename T, bool COMP>
+// LO = false (compensated storage only): hi = fl(x) and lo = 0, for a field that the Gauss projection
+// takes next -- its sweeps read the hi parts only and clear the lo parts when they finish -- so the
+// three FP64 operations per value of the exact lo are not spent.
+template <int D, typename T, bool COMP, bool LO = true>
 __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restrict__ aos, T *__restrict__ E,
                                                          uint32_t V, size_t elo) {
     // one thread per link, the D directions of a site on consecutive threads: a warp reads 2 KB of the
@@ -1044,8 +1047,15 @@ __global__ void __launch_bounds__(128) k_efield_from_aos(const double *__restric
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const double2 v = __ldg(src + j);
-        split(v.x, h[2 * j], l[2 * j]);
-        split(v.y, h[2 * j + 1], l[2 * j + 1]);
+        if (LO) {
+            split(v.x, h[2 * j], l[2 * j]);
+            split(v.y, h[2 * j + 1], l[2 * j + 1]);
+        } else {
+            h[2 * j] = (T)v.x;
+            h[2 * j + 1] = (T)v.y;
+            l[2 * j] = T(0);
+            l[2 * j + 1] = T(0);
+        }
     }
     const size_t ei = tix(site, D * 8, mu * 8);
     store_efield<T>(E, ei, h);

@@ -1096,8 +1096,15 @@ int lq_hmc_refresh(lq_state *s, uint64_t seed, uint64_t counter, int max_gauss_s
 int lq_hmc_refresh_upload(lq_state *s, const double *efield_raw, size_t n, int max_gauss_steps, int *gauss_steps) {
     LQ_CHECK_STATE(s);
     if (!valid_std_dev(0.5 / s->beta)) return LQ_ERR_INVALID_NORMAL;
-    int rc = lq_efield_upload(s, efield_raw, n);
+    if (!efield_raw) return LQ_ERR_INVALID_ARGUMENT;
+    if (n != (size_t)s->V * s->dim * 8) return LQ_ERR_INCOMPATIBLE_SIZE;
+    const size_t bytes = n * sizeof(double);
+    int rc = ensure_staging(*s, bytes);
     if (rc) return rc;
+    LQ_CK(cudaMemcpyAsync(s->staging, efield_raw, bytes, cudaMemcpyHostToDevice, s->stream));
+    // the projection below reads the hi parts and clears the lo parts
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_hi_from_aos(*s, (const double *)s->staging));
+    s->has_pending = 0;
     s->leap = 0;
     s->t = 0;
     return project_gauss(*s, max_gauss_steps, gauss_steps);
@@ -1135,7 +1142,8 @@ int lq_hmc_refresh_prefetched(lq_state *s, int max_gauss_steps, int *gauss_steps
     if (!s->prefetch_pending) return LQ_ERR_NO_PENDING;
     if (!valid_std_dev(0.5 / s->beta)) return LQ_ERR_INVALID_NORMAL;
     LQ_CK(cudaStreamWaitEvent(s->stream, s->prefetch_done, 0));
-    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_from_aos(*s, (const double *)s->prefetch));
+    // the projection below reads the hi parts and clears the lo parts
+    LQ_LAUNCH(*s, LQ_KERNEL_OTHER, s->ops->efield_hi_from_aos(*s, (const double *)s->prefetch));
     LQ_CK(cudaEventRecord(s->prefetch_free, s->stream));
     s->prefetch_pending = 0;
     s->has_pending = 0;

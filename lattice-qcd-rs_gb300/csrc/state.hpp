@@ -147,6 +147,9 @@ struct Ops {
     // one checkerboard class of a Metropolis (0) / heat-bath (1) sweep, in place
     cudaError_t (*mc_sweep)(State &s, void *U, int alg, int mu, int parity, double beta, uint64_t seed,
                             uint64_t sweep, int n_update, double spread, uint32_t *n_partials);
+    // E <- a field in the reference layout that the Gauss projection takes next: hi parts only, lo
+    // parts cleared (the projection reads hi and clears lo itself); as efield_from_aos without COMP
+    cudaError_t (*efield_hi_from_aos)(State &s, const double *d_aos);
 };
 
 const Ops *ops_f64(int dim);

@@ -214,13 +214,14 @@ def run_reference(args):
 NCU_MD_TRAFFIC_PER_LINK = {"mixed": 994.9e6 / 2458624}
 
 
-def algorithmic_md_bytes(n_links, md_steps, real_bytes):
+def algorithmic_md_bytes(n_links, md_steps, real_bytes, compensated=False):
     """Bytes moved by the fused MD kernels of one trajectory at ideal neighbour reuse.
     kick+drift launch: read U (18 reals) + E (8) + write E (8) + U' (18) = 52 reals per link;
-    final kick-only launch: read U (18) + E (8) + write E (8) = 34 reals per link.
+    final kick-only launch: read U (18) + E (8) + write E (8) = 34 reals per link, where the
+    compensated (mixed) form reads the link's hi half only (9 pair-sized units): 25.
     real_bytes is the stored size of one real: 8 for FP64 and for the compensated FP32 pairs
     of the mixed form, 4 for plain FP32 storage."""
-    return n_links * real_bytes * (52 * md_steps + 34)
+    return n_links * real_bytes * (52 * md_steps + (25 if compensated else 34))
 
 
 def rank_reducers(pg, device):
@@ -355,7 +356,7 @@ def run_ours(args):
     value = replica_value(n_links * nmd * args.steps, ms, max_over_ranks, sum_over_ranks)
     launches = sum(v[0] for v in prof.values())
     md_launches, md_ms = prof["md"]
-    md_bytes = algorithmic_md_bytes(n_links, nmd, real_bytes) * args.steps
+    md_bytes = algorithmic_md_bytes(n_links, nmd, real_bytes, prec == lqgpu.PRECISION_MIXED) * args.steps
     peak, peak_kind = measured_peaks()
     achieved = md_bytes / (md_ms / 1000.0) / 1e9 if md_ms > 0 else 0.0
     gauss_steps = [r["gauss_steps"] for r in res]

@@ -173,7 +173,8 @@ def scale_study(args):
             ms, prof, steps = time_trajectories(s, k, dt, nmd)
             md_n, md_ms = prof["md"]
             real = 8
-            md_bytes = n_links * real * (52 * nmd + 34) * k
+            # kick+drift launches 52 reals per link; the final kick 34, 25 in the mixed form (link hi only)
+            md_bytes = n_links * real * (52 * nmd + (25 if p == lqgpu.PRECISION_MIXED else 34)) * k
             row[PREC_NAMES[p]] = {"link_updates_per_s": n_links * nmd * k / (ms / 1e3), "ms_per_trajectory": ms / k,
                                   "gauss_steps": steps[0], "md_ms": md_ms / max(1, md_n),
                                   "md_hbm_gbs": md_bytes / (md_ms / 1e3) / 1e9 if md_ms else None,

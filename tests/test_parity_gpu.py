@@ -188,6 +188,30 @@ def test_hmc_trajectories_config1(oracle_mod, lqgpu_mod):
             assert abs(s.average_trace_plaquette() - O.average_trace_plaquette(dim, L, links)) <= TOL
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_config1_with_unit_normal_momenta(oracle_mod, lqgpu_mod, precision):
+    """The same workload with momenta N(0, 1) in every su(3) component, as the small configuration
+    words it (the reference's own draw is N(0, 0.5/beta)): the reference's Gauss projection
+    (relaxation 0.12 on a step quadratic in G) diverges at this spread, so the oracle returns
+    GaussProjectionError, and so does the library, in FP64 and in the mixed form."""
+    O, G = oracle_mod, lqgpu_mod
+    dim, L, size, beta, dt, nsteps = 4, 8, 1000.0, 1.0, 0.01, 10
+    rng = O.Rng(0)
+    links = O.links_random(dim, L, rng)
+    e_raw = O.efield_normal(dim, L, rng, 1.0)
+    with pytest.raises(O.OracleError) as err:
+        O.hmc_trajectory(dim, L, size, beta, links, e_raw, dt, nsteps, 0.5)
+    assert err.value.code == O.OR_ERR_GAUSS_PROJECTION
+    with G.State(dim, L, size, beta, precision) as s:
+        s.set_link_matrix(links)
+        with pytest.raises(G.LqError) as gerr:
+            s.hmc_refresh_upload(e_raw)
+        assert gerr.value.code == G.LQ_ERR_GAUSS_PROJECTION
+        # the links are untouched and the state stays usable: a draw at the reference's spread projects
+        assert rel(s.link_matrix(), links) <= TOL
+        s.hmc_refresh_upload(O.efield_normal(dim, L, rng, 0.5 / beta))
+
+
 def test_hmc_trajectory_device_rng(lqgpu_mod):
     """The device-RNG trajectory is deterministic in (seed, counter) and keeps links in SU(3)."""
     G = lqgpu_mod

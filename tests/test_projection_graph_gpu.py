@@ -103,6 +103,22 @@ def test_projection_graph_without_step_limit(lqgpu_mod, precision):
         assert np.array_equal(a.e_field(), b.e_field())
 
 
+@pytest.mark.parametrize("dim,Lt", [(2, 2), (2, 3), (3, 2), (3, 3), (4, 2), (4, 3)])
+def test_projection_graph_tiny_lattices(lqgpu_mod, dim, Lt):
+    """L = 2 (x + mu and x - mu coincide) and volumes that end inside a tile, D = 2, 3, 4: trajectories
+    with the graph equal those with the host loop."""
+    G = lqgpu_mod
+    a = G.State(dim, Lt, SIZE, BETA, G.PRECISION_MIXED)
+    b = G.State(dim, Lt, SIZE, BETA, G.PRECISION_MIXED)
+    with a, b:
+        a.set_links_random(7)
+        b.set_link_matrix(a.link_matrix())
+        b.set_projection_graph(False)
+        for k in range(3):
+            assert a.hmc_trajectory(0.01, 4, 3, k, 0.5) == b.hmc_trajectory(0.01, 4, 3, k, 0.5)
+        assert np.array_equal(a.link_matrix(), b.link_matrix())
+
+
 def test_projection_graph_profile_counts(lqgpu_mod):
     """The graph's profile slot counts the Gauss law, every sweep and every test."""
     G = lqgpu_mod

@@ -194,6 +194,14 @@ int lq_leapfrog_n(lq_state *s, double dt, int n);
 int lq_metropolis_sweep(lq_state *s, int n_update, double spread, uint64_t seed, uint64_t sweep,
                         long long *n_accepted, double *prob_mean);
 int lq_heat_bath_sweep(lq_state *s, uint64_t seed, uint64_t sweep);
+/* OverrelaxationSweepRotation (LQ_OVERRELAX_ROTATION) / OverrelaxationSweepReverse
+ * (LQ_OVERRELAX_REVERSE), src/simulation/monte_carlo/overrelaxation.rs: every link replaced by
+ * rot U^dag rot with rot = U_s V_s^dag, or by U_s reverse(U_s^dag U V_s) V_s^dag, from the singular
+ * value decomposition U_s S V_s^dag of the Monte Carlo staple's adjoint (reverse negates the
+ * off-diagonal entries); the link Hamiltonian is conserved.  Checkerboard order as the sweeps above
+ * (L even), arithmetic in double for every storage form; no random numbers. */
+enum { LQ_OVERRELAX_ROTATION = 0, LQ_OVERRELAX_REVERSE = 1 };
+int lq_overrelaxation_sweep(lq_state *s, int method);
 
 /* ---------------------------------------------------------------- clover observables
  * LinkMatrix::f_mu_nu and magnetic_field_vec (src/field.rs:822-871) at every site, from the clover

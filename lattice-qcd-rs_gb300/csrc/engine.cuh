@@ -216,14 +216,20 @@ template <int D, typename T, bool COMP> struct Engine {
                                 uint64_t sweep, int n_update, double spread, uint32_t *n_partials) {
         const uint32_t blocks = (s.V + 127) / 128;
         const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-        if (alg == MC_METROPOLIS)
-            k_mc_sweep<D, T, COMP, MC_METROPOLIS><<<blocks, 128, 0, s.stream>>>(
-                (V2<T> *)U, geo(s), mu, parity, beta, key, (uint32_t)sweep, (uint32_t)(sweep >> 32), n_update, spread,
-                s.partial);
-        else
-            k_mc_sweep<D, T, COMP, MC_HEAT_BATH><<<blocks, 128, 0, s.stream>>>(
-                (V2<T> *)U, geo(s), mu, parity, beta, key, (uint32_t)sweep, (uint32_t)(sweep >> 32), n_update, spread,
-                s.partial);
+#define LQ_MC_CASE(A)                                                                                                  \
+    case (A):                                                                                                          \
+        k_mc_sweep<D, T, COMP, (A)><<<blocks, 128, 0, s.stream>>>((V2<T> *)U, geo(s), mu, parity, beta, key,           \
+                                                                  (uint32_t)sweep, (uint32_t)(sweep >> 32), n_update, \
+                                                                  spread, s.partial);                                  \
+        break;
+        switch (alg) {
+            LQ_MC_CASE(MC_METROPOLIS)
+            LQ_MC_CASE(MC_HEAT_BATH)
+            LQ_MC_CASE(MC_OVERRELAX_ROTATION)
+            LQ_MC_CASE(MC_OVERRELAX_REVERSE)
+        default: return cudaErrorInvalidValue;
+        }
+#undef LQ_MC_CASE
         *n_partials = blocks;
         return cudaGetLastError();
     }

@@ -841,6 +841,13 @@ int lq_heat_bath_sweep(lq_state *s, uint64_t seed, uint64_t sweep) {
     return mc_sweep(s, lq::MC_HEAT_BATH, 1, 0.5, seed, sweep, nullptr, nullptr);
 }
 
+int lq_overrelaxation_sweep(lq_state *s, int method) {
+    LQ_CHECK_STATE(s);
+    if (method != LQ_OVERRELAX_ROTATION && method != LQ_OVERRELAX_REVERSE) return LQ_ERR_INVALID_ARGUMENT;
+    const int alg = method == LQ_OVERRELAX_ROTATION ? lq::MC_OVERRELAX_ROTATION : lq::MC_OVERRELAX_REVERSE;
+    return mc_sweep(s, alg, 1, 0.5, 0, 0, nullptr, nullptr);
+}
+
 // ------------------------------------------------------------------ differentiation
 int lq_wilson_action(lq_state *s, double *out) { return lq_hamiltonian_links(s, out); }
 

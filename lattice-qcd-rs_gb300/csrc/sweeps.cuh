@@ -256,10 +256,162 @@ __device__ __forceinline__ void mc_staple(const V2<T> *__restrict__ U, size_t ul
     }
 }
 
-enum : int { MC_METROPOLIS = 0, MC_HEAT_BATH = 1 };
+enum : int { MC_METROPOLIS = 0, MC_HEAT_BATH = 1, MC_OVERRELAX_ROTATION = 2, MC_OVERRELAX_REVERSE = 3 };
+
+// ---- overrelaxation (src/simulation/monte_carlo/overrelaxation.rs), in double ----
+// Both methods use the singular value decomposition a = U S V^dag of a = staple^dag (nalgebra's SVD
+// in the reference), taken here from the eigen-decomposition of the Hermitian a^dag a = V S^2 V^dag
+// by cyclic complex Jacobi rotations (Golub & Van Loan, Matrix Computations, section 8.5: the phase
+// of the off-diagonal element removed first, then the real rotation with
+// tan 2 theta = 2 |h_pq| / (h_qq - h_pp)), 8 sweeps over the pairs (0,1), (0,2), (1,2), and
+// U = a V S^-1.  For distinct singular values both updates are independent of the SVD's phase and
+// ordering freedom, so they are the reference's:
+//   rotation (:92-104): rot = U V^dag, U' = rot U^dag rot
+//   reverse  (:160-172): U' = U reverse(U^dag L V) V^dag, reverse negating the off-diagonal entries
+//                        (su3.rs:705-714)
+// The update divides by the smallest singular value of the staple and so magnifies rounding
+// differences; everything here, the staple included, is evaluated in the operation order of the
+// oracle's restatement with separately rounded products and sums (no fused multiply-add), which keeps
+// the FP64 form equal to it.
+struct XD {
+    // complex arithmetic as the textbook product and sum, each operation rounded
+    static __device__ __forceinline__ cpx<double> mul(cpx<double> a, cpx<double> b) {
+        return cmk(__dsub_rn(__dmul_rn(a.re, b.re), __dmul_rn(a.im, b.im)),
+                   __dadd_rn(__dmul_rn(a.re, b.im), __dmul_rn(a.im, b.re)));
+    }
+    static __device__ __forceinline__ cpx<double> add(cpx<double> a, cpx<double> b) {
+        return cmk(__dadd_rn(a.re, b.re), __dadd_rn(a.im, b.im));
+    }
+    // r = a b, each entry summed over k = 0, 1, 2 in that order
+    static __device__ void mm(const mat3<double> &a, const mat3<double> &b, mat3<double> &r) {
+        mat3<double> t;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                cpx<double> x = mul(a.e[i * 3], b.e[j]);
+                x = add(x, mul(a.e[i * 3 + 1], b.e[3 + j]));
+                x = add(x, mul(a.e[i * 3 + 2], b.e[6 + j]));
+                t.e[i * 3 + j] = x;
+            }
+        r = t;
+    }
+    static __device__ __forceinline__ void adj(const mat3<double> &a, mat3<double> &r) {
+        mat3<double> t;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) t.e[i * 3 + j] = cmk(a.e[j * 3 + i].re, -a.e[j * 3 + i].im);
+        r = t;
+    }
+    static __device__ __forceinline__ void madd(const mat3<double> &a, const mat3<double> &b, mat3<double> &r) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) r.e[k] = add(a.e[k], b.e[k]);
+    }
+};
+
+// the Monte Carlo staple of mc_staple, in the oracle's order: for nu != mu ascending,
+//   sum += ((U_nu(x) U_mu(x+nu)) U_nu(x+mu)^dag)^dag + (U_nu(x+mu-nu)^dag U_mu(x-nu)^dag) U_nu(x-nu)
+template <int D, typename T, bool COMP>
+__device__ void mc_staple_exact(const V2<T> *__restrict__ U, size_t ulo, const Geo<D> &g, uint32_t site,
+                                const uint32_t *c, int mu, mat3<double> &sum) {
+    const uint32_t xpmu = fwd(g, site, c[mu], mu);
+    mat_zero(sum);
+#pragma unroll 1
+    for (int nu = 0; nu < D; ++nu) {
+        if (nu == mu) continue;
+        mat3<double> a, b, t, el1, u1, u2, term;
+        load_link_d<T, COMP>(U, ulo, tix(site, D * 9, nu * 9), a);
+        load_link_d<T, COMP>(U, ulo, tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), b);
+        XD::mm(a, b, t);
+        load_link_d<T, COMP>(U, ulo, tix(xpmu, D * 9, nu * 9), a);
+        XD::adj(a, b);
+        XD::mm(t, b, a);
+        XD::adj(a, el1);
+        const uint32_t xmnu = bwd(g, site, c[nu], nu);
+        load_link_d<T, COMP>(U, ulo, tix(bwd(g, xpmu, c[nu], nu), D * 9, nu * 9), a);
+        XD::adj(a, u1);
+        load_link_d<T, COMP>(U, ulo, tix(xmnu, D * 9, mu * 9), a);
+        XD::adj(a, u2);
+        XD::mm(u1, u2, t);
+        load_link_d<T, COMP>(U, ulo, tix(xmnu, D * 9, nu * 9), a);
+        XD::mm(t, a, term);
+        XD::madd(el1, term, term);
+        XD::madd(sum, term, sum);
+    }
+}
+
+__device__ inline void herm3_eigen_jacobi(mat3<double> h, double (&lam)[3], mat3<double> &v) {
+    mat_identity(v);
+#pragma unroll 1
+    for (int sweep = 0; sweep < 8; ++sweep)
+#pragma unroll 1
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            const cpx<double> hpq = h.e[p * 3 + q];
+            const double c = sqrt(__dadd_rn(__dmul_rn(hpq.re, hpq.re), __dmul_rn(hpq.im, hpq.im)));
+            if (!(c > 0.0)) continue;
+            const cpx<double> ph = cmk(hpq.re / c, hpq.im / c); // e^{i phi}
+            const double tau = __dsub_rn(h.e[q * 4].re, h.e[p * 4].re) / (2.0 * c);
+            const double t =
+                (tau >= 0.0 ? 1.0 : -1.0) / __dadd_rn(fabs(tau), sqrt(__dadd_rn(1.0, __dmul_rn(tau, tau))));
+            const double cs = 1.0 / sqrt(__dadd_rn(1.0, __dmul_rn(t, t))), sn = __dmul_rn(t, cs);
+            // J: identity except J_pp = cs, J_pq = sn, J_qp = -sn e^{-i phi}, J_qq = cs e^{-i phi}
+            mat3<double> j, ja, x;
+            mat_identity(j);
+            j.e[p * 4] = cmk(cs, 0.0);
+            j.e[p * 3 + q] = cmk(sn, 0.0);
+            const cpx<double> phc = cmk(ph.re, -ph.im);
+            j.e[q * 3 + p] = XD::mul(phc, cmk(-sn, 0.0));
+            j.e[q * 4] = XD::mul(phc, cmk(cs, 0.0));
+            XD::adj(j, ja);
+            XD::mm(ja, h, x);
+            XD::mm(x, j, h);
+            XD::mm(v, j, v);
+        }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) lam[k] = h.e[k * 4].re;
+}
+__device__ inline mat3<double> overrelax_link(const mat3<double> &link, const mat3<double> &staple, int method) {
+    mat3<double> a, h, v, u, av, r, x, y;
+    XD::adj(staple, a);
+    XD::adj(a, x);
+    XD::mm(x, a, h); // a^dag a
+    double lam[3];
+    herm3_eigen_jacobi(h, lam, v);
+    XD::mm(a, v, av);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double sv = sqrt(fmax(lam[k], 0.0));
+#pragma unroll
+        for (int i = 0; i < 3; ++i) u.e[i * 3 + k] = cmk(av.e[i * 3 + k].re / sv, av.e[i * 3 + k].im / sv);
+    }
+    if (method == MC_OVERRELAX_ROTATION) {
+        mat3<double> rot;
+        XD::adj(v, x);
+        XD::mm(u, x, rot); // U V^dag
+        XD::adj(link, x);
+        XD::mm(rot, x, y); // rot U^dag
+        XD::mm(y, rot, r);
+        return r;
+    }
+    XD::adj(u, x);
+    XD::mm(x, link, y); // U^dag L
+    XD::mm(y, v, x);    // U^dag L V
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            if (i != j) x.e[i * 3 + j] = cmk(-x.e[i * 3 + j].re, -x.e[i * 3 + j].im);
+    XD::mm(u, x, y);
+    XD::adj(v, x);
+    XD::mm(y, x, r); // U reverse(...) V^dag
+    return r;
+}
 
 // One checkerboard class of a sweep: links (x, mu) with parity(x) = parity.  Metropolis partials:
-// row 0 accepted count, row 1 sum of acceptance probabilities (per block).
+// row 0 accepted count, row 1 sum of acceptance probabilities (per block).  The overrelaxation
+// updates draw no random numbers.
 template <int D, typename T, bool COMP, int ALG>
 __global__ void __launch_bounds__(128) k_mc_sweep(V2<T> *__restrict__ U, Geo<D> g, int mu, int parity, double beta,
                                                   uint2 key, uint32_t s_lo, uint32_t s_hi, int n_update,
@@ -311,6 +463,12 @@ __global__ void __launch_bounds__(128) k_mc_sweep(V2<T> *__restrict__ U, Geo<D> 
                 store_link_d<T, COMP>(U, ulo, ui, nm);
                 v[0] = 1.0;
             }
+        } else if (ALG == MC_OVERRELAX_ROTATION || ALG == MC_OVERRELAX_REVERSE) {
+            // OverrelaxationSweepRotation / OverrelaxationSweepReverse::get_modif (overrelaxation.rs:92-104,
+            // :160-172) with the Monte Carlo staple
+            mc_staple_exact<D, T, COMP>(U, ulo, g, site, c, mu, a);
+            out = overrelax_link(u, a, ALG);
+            store_link_d<T, COMP>(U, ulo, ui, out);
         } else {
             // HeatBathSweep::get_modif (heat_bath.rs:88-108): U' = t s r U
             mc_staple<D, T, COMP>(U, ulo, g, site, c, mu, a);

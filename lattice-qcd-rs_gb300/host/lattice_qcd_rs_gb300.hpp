@@ -510,6 +510,27 @@ template <class Rng = Xoshiro256PlusPlus> class HeatBathSweep {
     uint64_t sweep_ = 0;
 };
 
+// OverrelaxationSweepRotation / OverrelaxationSweepReverse (overrelaxation.rs:77-205): no random
+// numbers; MonteCarlo::next_element with Error = Never in the reference (device errors here).
+class OverrelaxationSweepRotation {
+  public:
+    template <int D> Result<LatticeStateDefault<D>> next_element(LatticeStateDefault<D> state) {
+        const int rc = lq_overrelaxation_sweep(state.raw(), LQ_OVERRELAX_ROTATION);
+        if (rc) return Result<LatticeStateDefault<D>>::err(rc);
+        state.invalidate_mirror();
+        return Result<LatticeStateDefault<D>>::ok(std::move(state));
+    }
+};
+class OverrelaxationSweepReverse {
+  public:
+    template <int D> Result<LatticeStateDefault<D>> next_element(LatticeStateDefault<D> state) {
+        const int rc = lq_overrelaxation_sweep(state.raw(), LQ_OVERRELAX_REVERSE);
+        if (rc) return Result<LatticeStateDefault<D>>::err(rc);
+        state.invalidate_mirror();
+        return Result<LatticeStateDefault<D>>::ok(std::move(state));
+    }
+};
+
 template <int D, class Rng = Xoshiro256PlusPlus, class I = SymplecticEulerGpu> class HybridMonteCarloDiagnostic {
   public:
     HybridMonteCarloDiagnostic(Real delta_t, std::size_t number_of_steps, I integrator, Rng rng)

@@ -33,6 +33,7 @@ PRECISION_MIXED = 1
 PRECISION_F32 = 2
 SYNC_SYNC, SYNC_LEAP, LEAP_LEAP, LEAP_SYNC, SYMPLECTIC, SYMPLECTIC_EXP, SYMPLECTIC_EXP_REUNITARIZE = range(7)
 LINK_UPDATE_EULER, LINK_UPDATE_EXP, LINK_UPDATE_EXP_REUNITARIZE = range(3)
+OVERRELAX_ROTATION, OVERRELAX_REVERSE = range(2)
 BATCH_USE_GRAPH, BATCH_MEASURE_PLAQUETTE = 1, 2
 BATCH_KERNEL_CLASSES = ("md", "sweep", "gauss", "plaquette_delta", "sumsq_delta", "normal", "plaquette")
 
@@ -83,6 +84,7 @@ SIGNATURES = {
     "lq_link_rotate": (_i32, [_vp, ctypes.c_longlong, _i32, _f64]),
     "lq_metropolis_sweep": (_i32, [_vp, _i32, _f64, _u64, _u64, _llp, _dp]),
     "lq_heat_bath_sweep": (_i32, [_vp, _u64, _u64]),
+    "lq_overrelaxation_sweep": (_i32, [_vp, _i32]),
     "lq_field_strength": (_i32, [_vp, _dp, _sz]),
     "lq_magnetic_field": (_i32, [_vp, _dp, _sz]),
     "lq_leapfrog_adjoint": (_i32, [_vp, _f64, _i32, _i32, _dp, _dp, _dp, _sz, _dp, _sz, _szp]),
@@ -302,6 +304,11 @@ class State:
         _check(load().lq_metropolis_sweep(self._h, n_update, spread, seed, sweep, ctypes.byref(acc),
                                           ctypes.byref(pm)), "lq_metropolis_sweep")
         return acc.value, pm.value
+
+    def overrelaxation_sweep(self, method):
+        """one checkerboard OverrelaxationSweepRotation (OVERRELAX_ROTATION) or
+        OverrelaxationSweepReverse (OVERRELAX_REVERSE)"""
+        _check(load().lq_overrelaxation_sweep(self._h, method), "lq_overrelaxation_sweep")
 
     def heat_bath_sweep(self, seed, sweep):
         """one checkerboard HeatBathSweep"""

@@ -934,6 +934,72 @@ int check_lattice(int dim, long L) {
     return OR_OK;
 }
 
+/* ---- overrelaxation (src/simulation/monte_carlo/overrelaxation.rs) ----
+ * Both methods use the singular value decomposition a = U S V^dag of a = staple^dag (nalgebra's
+ * SVD, not vendored).  Restated from the eigen-decomposition of the Hermitian a^dag a = V S^2 V^dag
+ * by cyclic complex Jacobi rotations (Golub & Van Loan, Matrix Computations, section 8.5; the phase
+ * of the off-diagonal element is removed first, then the real rotation with
+ * tan 2 theta = 2 |h_pq| / (h_qq - h_pp)), 8 sweeps over the pairs (0,1), (0,2), (1,2), and
+ * U = a V S^-1.  For distinct singular values both updates are independent of the SVD's phase and
+ * ordering freedom (a diagonal phase or a permutation commutes through `reverse`), so they are the
+ * reference's values.  The device evaluates the same operations in the same order without fused
+ * multiply-adds (the update divides by the smallest singular value, so it magnifies rounding
+ * differences; identical arithmetic keeps FP64 parity at 1e-12):
+ *   rotation (:92-104): rot = U V^dag, U' = rot U^dag rot
+ *   reverse  (:160-172): U' = U reverse(U^dag L V) V^dag, reverse negating the off-diagonal entries
+ *                        (su3.rs:705-714)
+ */
+void herm3_eigen_jacobi(M3 h, double lam[3], M3 &v) {
+    v = identity3();
+    const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int sweep = 0; sweep < 8; ++sweep)
+        for (const auto &pq : pairs) {
+            const int p = pq[0], q = pq[1];
+            /* sqrt of the sum of squares, not hypot, so that the device can evaluate it identically */
+            const double c = std::sqrt(h.m[p][q].re * h.m[p][q].re + h.m[p][q].im * h.m[p][q].im);
+            if (!(c > 0.0)) continue;
+            const Cx ph = cx(h.m[p][q].re / c, h.m[p][q].im / c); /* e^{i phi} */
+            const double tau = (h.m[q][q].re - h.m[p][p].re) / (2.0 * c);
+            const double t = (tau >= 0.0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+            const double cs = 1.0 / std::sqrt(1.0 + t * t), sn = t * cs;
+            /* J = identity except J_pp = cs, J_pq = sn, J_qp = -sn e^{-i phi}, J_qq = cs e^{-i phi} */
+            M3 j = identity3();
+            j.m[p][p] = cx(cs);
+            j.m[p][q] = cx(sn);
+            j.m[q][p] = conj(ph) * cx(-sn);
+            j.m[q][q] = conj(ph) * cx(cs);
+            h = (adjoint(j) * h) * j;
+            v = v * j;
+        }
+    for (int k = 0; k < 3; ++k) lam[k] = h.m[k][k].re;
+}
+/* U and V of a = U S V^dag, S from the eigenvalues of a^dag a */
+void svd3(const M3 &a, M3 &u, M3 &v) {
+    double lam[3];
+    herm3_eigen_jacobi(adjoint(a) * a, lam, v);
+    const M3 av = a * v;
+    for (int k = 0; k < 3; ++k) {
+        const double s = std::sqrt(std::fmax(lam[k], 0.0));
+        for (int i = 0; i < 3; ++i) u.m[i][k] = cx(av.m[i][k].re / s, av.m[i][k].im / s);
+    }
+}
+M3 reverse3(const M3 &x) {
+    M3 r = x;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (i != j) r.m[i][j] = cx(-x.m[i][j].re, -x.m[i][j].im);
+    return r;
+}
+M3 overrelax_link(const M3 &link, const M3 &staple, int method) {
+    M3 u, v;
+    svd3(adjoint(staple), u, v);
+    if (method == 0) {
+        const M3 rot = u * adjoint(v);
+        return (rot * adjoint(link)) * rot;
+    }
+    return (u * reverse3((adjoint(u) * link) * v)) * adjoint(v);
+}
+
 } // namespace
 
 /* ======================= C interface ======================= */
@@ -1121,6 +1187,31 @@ int or_heat_bath_sweep(int dim, int L, double beta, const double *links_in, uint
             }
     return OR_OK;
 }
+/* OverrelaxationSweepRotation (method 0) / OverrelaxationSweepReverse (1) in checkerboard order:
+ * for each mu, the links (x, mu) with even, then odd sum of coordinates (the device order; the
+ * reference updates one link after another in lattice order) */
+int or_overrelaxation_sweep(int dim, int L, const double *links_in, int method, double *links_out) {
+    const int st = check_lattice(dim, L);
+    if (st) return st;
+    if (L % 2 != 0 || (method != 0 && method != 1)) return OR_ERR_INVALID_ARGUMENT;
+    const Lattice lat(dim, L);
+    std::memcpy(links_out, links_in, sizeof(double) * 18 * lat.V * dim);
+    for (int mu = 0; mu < dim; ++mu)
+        for (long parity = 0; parity < 2; ++parity)
+            for (long site = 0; site < lat.V; ++site) {
+                if (parity_of(lat, site) != parity) continue;
+                double *lp = links_out + (site * dim + mu) * 18;
+                store_m3(overrelax_link(load_m3(lp), mc_staple(lat, links_out, site, mu), method), lp);
+            }
+    return OR_OK;
+}
+/* one link's update from its link and staple matrices (18 doubles each, reference layout) */
+int or_overrelax_link(const double *link18, const double *staple18, int method, double *out18) {
+    if (method != 0 && method != 1) return OR_ERR_INVALID_ARGUMENT;
+    store_m3(overrelax_link(load_m3(link18), load_m3(staple18), method), out18);
+    return OR_OK;
+}
+
 int or_gauss(int dim, int L, const double *links, const double *efield, long site, double *out18) {
     const int st = check_lattice(dim, L);
     if (st) return st;

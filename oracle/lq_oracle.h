@@ -85,6 +85,10 @@ int or_metropolis_sweep(int dim, int L, double beta, const double *links_in, int
                         uint64_t seed, uint64_t sweep, double *links_out, long *n_accepted, double *prob_sum);
 int or_heat_bath_sweep(int dim, int L, double beta, const double *links_in, uint64_t seed, uint64_t sweep,
                        double *links_out);
+/* OverrelaxationSweepRotation (method 0) / OverrelaxationSweepReverse (1) in checkerboard order, and
+ * one link's update from its link and staple matrices (see the source) */
+int or_overrelaxation_sweep(int dim, int L, const double *links_in, int method, double *links_out);
+int or_overrelax_link(const double *link18, const double *staple18, int method, double *out18);
 int or_gauss(int dim, int L, const double *links, const double *efield, long site, double *out18);
 int or_gauss_sum_div(int dim, int L, const double *links, const double *efield, double *out);
 int or_project_to_gauss(int dim, int L, const double *links, const double *efield_in,

@@ -71,6 +71,8 @@ def lib():
             "or_metropolis_sweep": (i32, [i32, i32, ctypes.c_double, _dp, i32, ctypes.c_double, u64, u64, _dp,
                                           ctypes.POINTER(ctypes.c_long), _dp]),
             "or_heat_bath_sweep": (i32, [i32, i32, ctypes.c_double, _dp, u64, u64, _dp]),
+            "or_overrelaxation_sweep": (i32, [i32, i32, _dp, i32, _dp]),
+            "or_overrelax_link": (i32, [_dp, _dp, i32, _dp]),
             "or_f_mu_nu": (i32, [i32, i32, ctypes.c_double, _dp, lng, i32, i32, _dp]),
             "or_magnetic_field": (i32, [i32, i32, ctypes.c_double, _dp, lng, i32, _dp]),
             "or_gauss_sum_div": (i32, [i32, i32, _dp, _dp, _dp]),
@@ -247,6 +249,23 @@ def heat_bath_sweep(dim, L, beta, links, seed, sweep):
     out = np.zeros_like(links)
     _check(lib().or_heat_bath_sweep(dim, L, beta, _p(np.ascontiguousarray(links)), seed, sweep, _p(out)),
            "heat_bath_sweep")
+    return out
+
+
+def overrelaxation_sweep(dim, L, links, method):
+    """checkerboard OverrelaxationSweepRotation (method 0) / OverrelaxationSweepReverse (1)"""
+    out = np.zeros_like(links)
+    _check(lib().or_overrelaxation_sweep(dim, L, _p(np.ascontiguousarray(links)), method, _p(out)),
+           "overrelaxation_sweep")
+    return out
+
+
+def overrelax_link(link18, staple18, method):
+    """one link's overrelaxation update from its link and staple matrices (18 doubles each)"""
+    out = np.zeros(18)
+    _check(lib().or_overrelax_link(_p(np.ascontiguousarray(link18, dtype=np.float64)),
+                                   _p(np.ascontiguousarray(staple18, dtype=np.float64)), method, _p(out)),
+           "overrelax_link")
     return out
 
 

@@ -434,8 +434,8 @@ def tour_study(args):
     DRAM bytes under ncu): D = 4 states at L^4 (default 32^4: links and momenta above L2) in FP64,
     mixed and f32 -- conversions, momentum draws, Gauss law, projection (host-driven loop, so that
     profilers see its kernels), the MD modes and the exponential update, the HMC proposal, the action and
-    its backward, a link rotation, normalisation, clover fields, Metropolis and heat-bath sweeps and the
-    trajectory adjoint -- a D = 3 (128^3) and a D = 2 (2048^2) trajectory, the allocation-free plaquette
+    its backward, a link rotation, normalisation, clover fields, Metropolis, heat-bath and overrelaxation sweeps
+    and the trajectory adjoint -- a D = 3 (128^3) and a D = 2 (2048^2) trajectory, the allocation-free plaquette
     sums, and a batch of 8 uneven ensembles (L 16 .. 28, 9.4 M links) run eagerly."""
     import ctypes
 
@@ -473,6 +473,8 @@ def tour_study(args):
             s.magnetic_field()
             s.metropolis_sweep(1, 0.1, 3, 0)
             s.heat_bath_sweep(3, 1)
+            s.overrelaxation_sweep(lqgpu.OVERRELAX_ROTATION)
+            s.overrelaxation_sweep(lqgpu.OVERRELAX_REVERSE)
             s.leapfrog_adjoint(dt, 4)
         done.append(PREC_NAMES[prec])
     for dim, Ld in ((3, 128), (2, 2048)):

@@ -123,6 +123,14 @@ int main() {
         CHECK(std::isfinite(st.average_trace_plaquette().value().real()));
         auto odd = LatticeStateDefault<4>::new_cold(1.0, 8.0, 3).unwrap();
         CHECK(hb.next_element(std::move(odd)).error() == LQ_ERR_INVALID_ARGUMENT);
+        // overrelaxation after the heat bath, as the reference's module example does: the link
+        // Hamiltonian is conserved
+        OverrelaxationSweepReverse orr;
+        OverrelaxationSweepRotation orot;
+        const double h = st.hamiltonian_links();
+        st = std::move(st).monte_carlo_step(orr).unwrap();
+        st = std::move(st).monte_carlo_step(orot).unwrap();
+        CHECK(std::fabs(st.hamiltonian_links() - h) <= 1e-10 * std::fabs(h));
     }
 
     // setter with a wrong size panics, as the reference's set_link_matrix does

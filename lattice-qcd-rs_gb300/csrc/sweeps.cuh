@@ -341,34 +341,50 @@ __device__ void mc_staple_exact(const V2<T> *__restrict__ U, size_t ulo, const G
     }
 }
 
+// One Jacobi rotation J in the (P, Q) plane: h <- (J^dag h) J, v <- v J, with J the identity except
+// J_PP = cs, J_PQ = sn, J_QP = -sn e^{-i phi}, J_QQ = cs e^{-i phi}.  Only rows P, Q of J^dag h and
+// then columns P, Q change; the other entries of the full products are exact products with 1 and sums
+// with zeros, so updating just these entries, each in the full product's order, gives the same values.
+template <int P, int Q> __device__ __forceinline__ void jacobi_rotate(mat3<double> &h, mat3<double> &v) {
+    const cpx<double> hpq = h.e[P * 3 + Q];
+    const double c = sqrt(__dadd_rn(__dmul_rn(hpq.re, hpq.re), __dmul_rn(hpq.im, hpq.im)));
+    if (!(c > 0.0)) return;
+    const cpx<double> phc = cmk(hpq.re / c, -(hpq.im / c)); // e^{-i phi}
+    const double tau = __dsub_rn(h.e[Q * 4].re, h.e[P * 4].re) / (2.0 * c);
+    const double t = (tau >= 0.0 ? 1.0 : -1.0) / __dadd_rn(fabs(tau), sqrt(__dadd_rn(1.0, __dmul_rn(tau, tau))));
+    const double cs = 1.0 / sqrt(__dadd_rn(1.0, __dmul_rn(t, t))), sn = __dmul_rn(t, cs);
+    const cpx<double> jpp = cmk(cs, 0.0), jpq = cmk(sn, 0.0);
+    const cpx<double> jqp = XD::mul(phc, cmk(-sn, 0.0)), jqq = XD::mul(phc, cmk(cs, 0.0));
+    // conjugates: (J^dag)_PP, (J^dag)_PQ = conj(J_QP), (J^dag)_QP = conj(J_PQ), (J^dag)_QQ
+    const cpx<double> app = cmk(jpp.re, -jpp.im), apq = cmk(jqp.re, -jqp.im), aqp = cmk(jpq.re, -jpq.im),
+                      aqq = cmk(jqq.re, -jqq.im);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { // rows P, Q of J^dag h
+        const cpx<double> hp = h.e[P * 3 + k], hq = h.e[Q * 3 + k];
+        h.e[P * 3 + k] = XD::add(XD::mul(app, hp), XD::mul(apq, hq));
+        h.e[Q * 3 + k] = XD::add(XD::mul(aqp, hp), XD::mul(aqq, hq));
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { // columns P, Q of (J^dag h) J
+        const cpx<double> xp = h.e[i * 3 + P], xq = h.e[i * 3 + Q];
+        h.e[i * 3 + P] = XD::add(XD::mul(xp, jpp), XD::mul(xq, jqp));
+        h.e[i * 3 + Q] = XD::add(XD::mul(xp, jpq), XD::mul(xq, jqq));
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { // columns P, Q of v J
+        const cpx<double> vp = v.e[i * 3 + P], vq = v.e[i * 3 + Q];
+        v.e[i * 3 + P] = XD::add(XD::mul(vp, jpp), XD::mul(vq, jqp));
+        v.e[i * 3 + Q] = XD::add(XD::mul(vp, jpq), XD::mul(vq, jqq));
+    }
+}
 __device__ inline void herm3_eigen_jacobi(mat3<double> h, double (&lam)[3], mat3<double> &v) {
     mat_identity(v);
 #pragma unroll 1
-    for (int sweep = 0; sweep < 8; ++sweep)
-#pragma unroll 1
-        for (int pq = 0; pq < 3; ++pq) {
-            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
-            const cpx<double> hpq = h.e[p * 3 + q];
-            const double c = sqrt(__dadd_rn(__dmul_rn(hpq.re, hpq.re), __dmul_rn(hpq.im, hpq.im)));
-            if (!(c > 0.0)) continue;
-            const cpx<double> ph = cmk(hpq.re / c, hpq.im / c); // e^{i phi}
-            const double tau = __dsub_rn(h.e[q * 4].re, h.e[p * 4].re) / (2.0 * c);
-            const double t =
-                (tau >= 0.0 ? 1.0 : -1.0) / __dadd_rn(fabs(tau), sqrt(__dadd_rn(1.0, __dmul_rn(tau, tau))));
-            const double cs = 1.0 / sqrt(__dadd_rn(1.0, __dmul_rn(t, t))), sn = __dmul_rn(t, cs);
-            // J: identity except J_pp = cs, J_pq = sn, J_qp = -sn e^{-i phi}, J_qq = cs e^{-i phi}
-            mat3<double> j, ja, x;
-            mat_identity(j);
-            j.e[p * 4] = cmk(cs, 0.0);
-            j.e[p * 3 + q] = cmk(sn, 0.0);
-            const cpx<double> phc = cmk(ph.re, -ph.im);
-            j.e[q * 3 + p] = XD::mul(phc, cmk(-sn, 0.0));
-            j.e[q * 4] = XD::mul(phc, cmk(cs, 0.0));
-            XD::adj(j, ja);
-            XD::mm(ja, h, x);
-            XD::mm(x, j, h);
-            XD::mm(v, j, v);
-        }
+    for (int sweep = 0; sweep < 8; ++sweep) {
+        jacobi_rotate<0, 1>(h, v);
+        jacobi_rotate<0, 2>(h, v);
+        jacobi_rotate<1, 2>(h, v);
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k) lam[k] = h.e[k * 4].re;
 }

@@ -17,6 +17,7 @@
 #include <complex>
 #include <cstdint>
 #include <memory>
+#include <functional>
 #include <optional>
 #include <stdexcept>
 #include <string>
@@ -529,6 +530,68 @@ class OverrelaxationSweepReverse {
         state.invalidate_mirror();
         return Result<LatticeStateDefault<D>>::ok(std::move(state));
     }
+};
+
+// HybridMethodCouple (src/simulation/monte_carlo/hybrid.rs:327-420): the first method, then the
+// second, on each step.  An error stops the step; error_position() tells which method raised it
+// (1: HybridMethodCoupleError::ErrorFirst, 2: ErrorSecond).
+template <class MC1, class MC2> class HybridMethodCouple {
+  public:
+    HybridMethodCouple(MC1 first, MC2 second) : first_(std::move(first)), second_(std::move(second)) {}
+    template <int D> Result<LatticeStateDefault<D>> next_element(LatticeStateDefault<D> state) {
+        error_position_ = 0;
+        auto r1 = first_.next_element(std::move(state));
+        if (r1.is_err()) {
+            error_position_ = 1;
+            return r1;
+        }
+        auto r2 = second_.next_element(r1.unwrap());
+        if (r2.is_err()) error_position_ = 2;
+        return r2;
+    }
+    int error_position() const { return error_position_; }
+    MC1 &first() { return first_; }
+    MC2 &second() { return second_; }
+
+  private:
+    MC1 first_;
+    MC2 second_;
+    int error_position_ = 0;
+};
+
+// HybridMethodVec (hybrid.rs:156-270): the referenced methods in order on each step (the reference
+// holds `&mut dyn MonteCarlo`; the caller keeps the methods alive here too).  No method: the
+// HybridMethodVecError::NoMethod case, LQ_ERR_INVALID_ARGUMENT with error_index() = -1; an error of
+// method i stops the step with error_index() = i (HybridMethodVecError::Error(i, e)).
+template <int D> class HybridMethodVec {
+  public:
+    using State = LatticeStateDefault<D>;
+    template <class M> void push_method(M &m) {
+        methods_.push_back([&m](State s) { return m.next_element(std::move(s)); });
+    }
+    void pop_method() {
+        if (!methods_.empty()) methods_.pop_back();
+    }
+    std::size_t len() const { return methods_.size(); }
+    bool is_empty() const { return methods_.empty(); }
+    Result<State> next_element(State state) {
+        error_index_ = -1;
+        if (methods_.empty()) return Result<State>::err(LQ_ERR_INVALID_ARGUMENT);
+        for (std::size_t i = 0; i < methods_.size(); ++i) {
+            auto r = methods_[i](std::move(state));
+            if (r.is_err()) {
+                error_index_ = (int)i;
+                return r;
+            }
+            state = r.unwrap();
+        }
+        return Result<State>::ok(std::move(state));
+    }
+    int error_index() const { return error_index_; }
+
+  private:
+    std::vector<std::function<Result<State>(State)>> methods_;
+    int error_index_ = -1;
 };
 
 template <int D, class Rng = Xoshiro256PlusPlus, class I = SymplecticEulerGpu> class HybridMonteCarloDiagnostic {

@@ -133,6 +133,33 @@ int main() {
         CHECK(std::fabs(st.hamiltonian_links() - h) <= 1e-10 * std::fabs(h));
     }
 
+    // HybridMethodCouple / HybridMethodVec (hybrid.rs): heat bath then overrelaxation per step, as
+    // the reference's module examples pair them; the errors name the failing method
+    {
+        HybridMethodCouple<HeatBathSweep<>, OverrelaxationSweepReverse> couple(
+            HeatBathSweep<>(Xoshiro256PlusPlus::seed_from_u64(3)), OverrelaxationSweepReverse());
+        auto st = LatticeStateDefault<3>::new_cold(1.0, 8.0, 4).unwrap();
+        for (int i = 0; i < 2; ++i) st = std::move(st).monte_carlo_step(couple).unwrap();
+        CHECK(std::isfinite(st.average_trace_plaquette().value().real()));
+        auto odd = LatticeStateDefault<3>::new_cold(1.0, 8.0, 3).unwrap();
+        CHECK(couple.next_element(std::move(odd)).error() == LQ_ERR_INVALID_ARGUMENT);
+        CHECK(couple.error_position() == 1);
+
+        HybridMethodVec<3> vec;
+        CHECK(vec.is_empty());
+        auto st2 = LatticeStateDefault<3>::new_cold(1.0, 8.0, 4).unwrap();
+        auto none = vec.next_element(std::move(st2));
+        CHECK(none.error() == LQ_ERR_INVALID_ARGUMENT && vec.error_index() == -1);
+        HeatBathSweep<> hb2(Xoshiro256PlusPlus::seed_from_u64(4));
+        OverrelaxationSweepRotation orot2;
+        vec.push_method(hb2);
+        vec.push_method(orot2);
+        CHECK(vec.len() == 2);
+        auto st3 = LatticeStateDefault<3>::new_cold(1.0, 8.0, 4).unwrap();
+        st3 = std::move(st3).monte_carlo_step(vec).unwrap();
+        CHECK(std::isfinite(st3.average_trace_plaquette().value().real()));
+    }
+
     // setter with a wrong size panics, as the reference's set_link_matrix does
     {
         auto s = LatticeStateDefault<2>::new_cold(1.0, 1.0, 4).unwrap();

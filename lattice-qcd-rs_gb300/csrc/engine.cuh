@@ -61,8 +61,9 @@ template <int D, typename T, bool COMP> struct Engine {
     static unsigned md_block_k() { return 128; }
     static cudaError_t force(State &s, const void *U, void *out, double scale) {
         const dim3 grid = md_grid_k(s);
-        k_md<D, T, COMP, MD_KICK><<<grid, md_block_k(), 0, s.stream>>>((const V2<T> *)U, (V2<T> *)U, (const T *)out, (T *)out,
-                                                               geo(s), T(0), (T)scale, T(0));
+        // kick only: the output links are never written (null)
+        k_md<D, T, COMP, MD_KICK><<<grid, md_block_k(), 0, s.stream>>>((const V2<T> *)U, (V2<T> *)nullptr, (const T *)out,
+                                                                       (T *)out, geo(s), T(0), (T)scale, T(0));
         return cudaGetLastError();
     }
     static cudaError_t link_rotate(State &s, void *U, uint32_t site, int mu, int a, double angle) {

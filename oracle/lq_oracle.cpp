@@ -393,7 +393,7 @@ struct Lattice {
     }
     /* add_point_direction_n with n = 1, src/lattice.rs:303-323 */
     long neighbour(long site, int mu, bool positive) const {
-        long x[4];
+        long x[4] = {0, 0, 0, 0};
         coords(site, x);
         if (positive) {
             x[mu] = (x[mu] + 1) % L;

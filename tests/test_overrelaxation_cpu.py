@@ -43,6 +43,22 @@ def test_link_update_matches_lapack_svd(oracle_mod, method):
     assert worst <= 1e-12, worst
 
 
+@pytest.mark.parametrize("eps", [1e-2, 1e-5, 1e-9, 0.0])
+def test_rotation_matches_lapack_on_near_degenerate_staples(oracle_mod, eps):
+    """Staples 6 W + eps X (W in SU(3)) have singular values eps apart, the slowest case for the
+    fixed number of Jacobi sweeps; the rotation's polar factor stays unique down to eps = 0."""
+    O = oracle_mod
+    rng = np.random.default_rng(31)
+    worst = 0.0
+    for _ in range(200):
+        link = np.linalg.qr(random_complex(rng))[0]
+        w = np.linalg.qr(random_complex(rng))[0]
+        staple = 6.0 * w / np.linalg.det(w) ** (1.0 / 3.0) + eps * random_complex(rng)
+        got = O.to_complex(O.overrelax_link(O.from_complex(link), O.from_complex(staple), 0))
+        worst = max(worst, np.abs(got - svd_update(link, staple, 0)).max())
+    assert worst <= 1e-12, worst
+
+
 @pytest.mark.parametrize("method", [0, 1])
 def test_link_update_is_an_involution(oracle_mod, method):
     O = oracle_mod

@@ -280,14 +280,27 @@ def batch_leg(args, stream, peak):
     b.close()
     md_bytes = links * 52 * 8
     ok = r["status"] == 0
+    # link updates of the trajectories whose projection succeeded: at the smallest betas the
+    # reference's projection diverges (its step is quadratic in the Gauss law) and its HMC refresh
+    # panics, so the work done on those ensembles is not counted
+    ens_links = np.asarray(Ls, dtype=np.int64) ** 4 * 4
+    counted = int((ok * ens_links[None, :]).sum()) * nmd
+    failed = {int(e): int((~ok[:, e]).sum()) for e in np.nonzero(~ok.all(axis=0))[0]}
     return {"workload": "64 ensembles D=4, L from {8,10,12,16,20} (seed 3), beta 0.5..3.5, size 1000, mixed, "
                         "10 leap-frog steps dt 0.01; one launch per kernel over all ensembles, one CUDA graph "
                         "per trajectory", "total_links": links, "trajectories": args.batch_traj,
-            "value": links * nmd * args.batch_traj / (ms / 1000.0), "unit": UNIT,
+            "value": counted / (ms / 1000.0), "unit": UNIT,
+            "counted": "link updates of ensemble trajectories whose Gauss projection succeeded",
+            "value_all_ensembles": links * nmd * args.batch_traj / (ms / 1000.0),
             "ms_per_trajectory": ms / args.batch_traj, "graph_launches": launches, "md_launch_ms": tuning["md"]["ms"],
             "md_hbm_frac": md_bytes / (tuning["md"]["ms"] / 1000.0) / 1e9 / peak,
             "tuning": {k: [v["grid"], v["order"]] for k, v in tuning.items()},
             "projection_failures": int((~ok).sum()),
+            "projection_failures_by_ensemble": [{"ensemble": e, "L": int(Ls[e]), "beta": round(float(betas[e]), 4),
+                                                 "trajectories": c} for e, c in failed.items()],
+            "projection_failure_cause": "NaN residual (LQ_ERR_GAUSS_PROJECTION): the reference's projection step is "
+                                        "quadratic in the Gauss law and diverges for momenta of standard deviation "
+                                        "0.5/beta near 1; the ensemble keeps its links",
             "acceptance": float(r["accepted"][ok].mean()) if ok.any() else None}
 
 

@@ -248,6 +248,21 @@ def replica_value(units, ms, max_over_ranks, sum_over_ranks):
     return sum_over_ranks(units) / (max_over_ranks(ms) / 1000.0)
 
 
+def counted_batch_link_updates(status, side_lengths, dim, md_steps):
+    """Link updates of the ensemble trajectories whose Gauss projection succeeded (status 0), from the
+    per-trajectory, per-ensemble status array [trajectories, ensembles]: at the smallest betas the
+    reference's projection diverges (its step is quadratic in the Gauss law) and its HMC refresh
+    panics, so the work done on those ensembles is not counted.  Also returns, per failing ensemble,
+    how many of its trajectories failed."""
+    import numpy as np
+
+    ok = np.asarray(status) == 0
+    ens_links = np.asarray(side_lengths, dtype=np.int64) ** dim * dim
+    counted = int((ok * ens_links[None, :]).sum()) * md_steps
+    failed = {int(e): int((~ok[:, e]).sum()) for e in np.nonzero(~ok.all(axis=0))[0]}
+    return counted, failed
+
+
 def batch_leg(args, stream, peak):
     """The parameter-scan workload: 64 ensembles, D = 4, side lengths drawn from {8, 10, 12, 16, 20}
     (seed 3), beta linearly spaced 0.5 .. 3.5, size 1000, mixed, 10 leap-frog steps dt 0.01; every
@@ -280,12 +295,7 @@ def batch_leg(args, stream, peak):
     b.close()
     md_bytes = links * 52 * 8
     ok = r["status"] == 0
-    # link updates of the trajectories whose projection succeeded: at the smallest betas the
-    # reference's projection diverges (its step is quadratic in the Gauss law) and its HMC refresh
-    # panics, so the work done on those ensembles is not counted
-    ens_links = np.asarray(Ls, dtype=np.int64) ** 4 * 4
-    counted = int((ok * ens_links[None, :]).sum()) * nmd
-    failed = {int(e): int((~ok[:, e]).sum()) for e in np.nonzero(~ok.all(axis=0))[0]}
+    counted, failed = counted_batch_link_updates(r["status"], Ls, 4, nmd)
     return {"workload": "64 ensembles D=4, L from {8,10,12,16,20} (seed 3), beta 0.5..3.5, size 1000, mixed, "
                         "10 leap-frog steps dt 0.01; one launch per kernel over all ensembles, one CUDA graph "
                         "per trajectory", "total_links": links, "trajectories": args.batch_traj,

@@ -43,6 +43,7 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "lattice-qcd-rs_gb300"))
 
 import lqgpu  # noqa: E402
+from bench import counted_batch_link_updates  # noqa: E402
 
 PREC_NAMES = {lqgpu.PRECISION_F64: "f64", lqgpu.PRECISION_MIXED: "mixed", lqgpu.PRECISION_F32: "f32"}
 
@@ -248,7 +249,7 @@ def batch_study(args):
            "device_bytes": info["device_bytes"], "autotune_seconds": round(tune_s, 2), "tuning": tuning,
            "ms_per_trajectory": ms / args.traj, "wall_s": wall,
            # trajectories whose projection failed (the reference's HMC refresh panics there) are not counted
-           "link_updates_per_s": int((ok * (np.asarray(Ls, dtype=np.int64) ** 4 * 4)[None, :]).sum()) * nmd / (ms / 1e3),
+           "link_updates_per_s": counted_batch_link_updates(r["status"], Ls, 4, nmd)[0] / (ms / 1e3),
            "link_updates_per_s_all_ensembles": links * nmd * args.traj / (ms / 1e3),
            "md_launch_ms": md_ms, "md_hbm_gbs": md_bytes / (md_ms / 1e3) / 1e9,
            "md_hbm_frac": md_bytes / (md_ms / 1e3) / 1e9 / peak,

@@ -45,3 +45,19 @@ def test_single_process_needs_no_group():
     barrier, mx, sm = bench.rank_reducers(None, None)
     barrier()
     assert bench.replica_value(10, 1000.0, mx, sm) == 10.0
+
+
+def test_batch_counts_only_successful_trajectories():
+    """the batch leg's throughput counts the links of ensemble trajectories whose projection
+    succeeded and names the ensembles that failed"""
+    import numpy as np
+
+    import bench
+
+    status = np.array([[0, 7, 0], [0, 7, 7], [0, 7, 0]])  # 3 trajectories x 3 ensembles
+    counted, failed = bench.counted_batch_link_updates(status, [2, 3, 4], 4, 10)
+    links = np.array([2, 3, 4]) ** 4 * 4
+    assert counted == (3 * links[0] + 0 * links[1] + 2 * links[2]) * 10
+    assert failed == {1: 3, 2: 1}
+    counted, failed = bench.counted_batch_link_updates(np.zeros((2, 2), dtype=int), [3, 5], 3, 1)
+    assert counted == 2 * (27 * 3 + 125 * 3) and failed == {}

@@ -435,16 +435,22 @@ template <int D, typename T, bool COMP, int ALG>
 __global__ void __launch_bounds__(128) k_mc_sweep(V2<T> *__restrict__ U, Geo<D> g, int mu, int parity, double beta,
                                                   uint2 key, uint32_t s_lo, uint32_t s_hi, int n_update,
                                                   double spread, double *__restrict__ partial) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    // one thread per site of the class (L is even): thread t takes row r = 2t / L (the sites with
+    // x1.. fixed) and there the j-th site, j = t - r L / 2, whose coordinate sum has the class's
+    // parity, so every lane of a warp has a link to update
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     double v[2] = {0.0, 0.0};
     uint32_t c[D];
-    bool active = site < g.V;
+    uint32_t site = 0;
+    const bool active = t < (g.V >> 1);
     if (active) {
-        site_coords(g, site, c);
-        uint32_t p = 0;
+        const uint32_t row = div_by_L(g, 2u * t);
+        site_coords(g, row * g.L, c); // c[0] = 0
+        uint32_t q = (uint32_t)parity;
 #pragma unroll
-        for (int i = 0; i < D; ++i) p += c[i];
-        active = (int)(p & 1u) == parity;
+        for (int i = 1; i < D; ++i) q += c[i];
+        c[0] = 2u * (t - row * (g.L >> 1)) + (q & 1u);
+        site = row * g.L + c[0];
     }
     if (active) {
         const size_t ulo = (size_t)tiles_of(g.V) * D * 9 * kTile;

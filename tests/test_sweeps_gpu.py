@@ -41,6 +41,31 @@ def test_heat_bath_matches_oracle(oracle_mod, lqgpu_mod, dim, L):
     assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
 
 
+@pytest.mark.parametrize("dim,L", [(4, 2), (4, 6), (3, 6), (2, 10), (2, 34)])
+def test_class_threads_cover_every_site_once(oracle_mod, lqgpu_mod, dim, L):
+    """Classes that need several blocks of threads, rows of sites that cross 32-site tiles (L = 6, 10,
+    34) and L = 2 (x + mu and x - mu coincide): a Metropolis then a heat-bath sweep, and an
+    overrelaxation sweep from the random start, equal the oracle's, so the threads of a class update
+    each of its links exactly once"""
+    O, G = oracle_mod, lqgpu_mod
+    beta = 2.5
+    links = O.links_random(dim, L, O.Rng(12))
+    with G.State(dim, L, 1.0, beta, G.PRECISION_F64) as s:
+        s.set_link_matrix(links)
+        ref, acc_ref, _ = O.metropolis_sweep(dim, L, beta, links, 1, 0.2, 5, 0)
+        acc, _ = s.metropolis_sweep(1, 0.2, 5, 0)
+        assert acc == acc_ref
+        ref = O.heat_bath_sweep(dim, L, beta, ref, 6, 0)
+        s.heat_bath_sweep(6, 0)
+        got = s.link_matrix()
+        assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+        s.set_link_matrix(links)
+        ref = O.overrelaxation_sweep(dim, L, links, 1)
+        s.overrelaxation_sweep(G.OVERRELAX_REVERSE)
+        got = s.link_matrix()
+    assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+
+
 def test_sweep_arguments(lqgpu_mod):
     G = lqgpu_mod
     with G.State(4, 3, 1.0, 2.0, G.PRECISION_F64) as s:  # odd L: no checkerboard

@@ -103,3 +103,23 @@ def test_batch_argument_validation_precedes_device_use(lqgpu_mod):
     assert lib.lq_batch_create(4, 0, None, None, None, 1, ctypes.byref(h)) == G.LQ_ERR_INVALID_ARGUMENT
     assert lib.lq_batch_hmc_run(None, 0.1, 1, 1, 0, 1) == G.LQ_ERR_INVALID_ARGUMENT
     assert lib.lq_batch_destroy(None) == G.LQ_OK
+
+
+def _param_counts(src, pattern):
+    counts = {}
+    for m in re.finditer(pattern, src, flags=re.S):
+        params = m.group(2).strip()
+        counts[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return counts
+
+
+def test_rust_binding_declares_every_function_with_its_arity():
+    """the -sys block of INTEGRATION.md binds every function of the header with as many parameters"""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    c = _param_counts(src, r"\b(lq_[a-z0-9_]+)\s*\(([^)]*)\)\s*;")
+    doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    block = doc[doc.index('extern "C" {'):]
+    block = block[:block.index("\n}\n")]
+    rust = _param_counts(block, r"pub fn (lq_[a-z0-9_]+)\(([^)]*)\)")
+    assert sorted(c) == sorted(rust), set(c) ^ set(rust)
+    assert {k: c[k] for k in c} == {k: rust[k] for k in c}

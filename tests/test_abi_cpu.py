@@ -113,8 +113,9 @@ def _param_counts(src, pattern):
     return counts
 
 
-def test_rust_binding_declares_every_function_with_its_arity():
-    """the -sys block of INTEGRATION.md binds every function of the header with as many parameters"""
+def test_bindings_declare_every_function_with_its_arity(lqgpu_mod):
+    """the ctypes table and the -sys block of INTEGRATION.md bind every function of the header with as
+    many parameters"""
     src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
     c = _param_counts(src, r"\b(lq_[a-z0-9_]+)\s*\(([^)]*)\)\s*;")
     doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
@@ -123,3 +124,4 @@ def test_rust_binding_declares_every_function_with_its_arity():
     rust = _param_counts(block, r"pub fn (lq_[a-z0-9_]+)\(([^)]*)\)")
     assert sorted(c) == sorted(rust), set(c) ^ set(rust)
     assert {k: c[k] for k in c} == {k: rust[k] for k in c}
+    assert {k: c[k] for k in c} == {k: len(lqgpu_mod.SIGNATURES[k][1]) for k in c}

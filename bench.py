@@ -464,20 +464,41 @@ def run_ours(args):
                 st.set_links_random(5)
             rngacc = np.random.default_rng(9)
             acc_out = {k: [] for k in states}
+            # Gauss-law residual gauss_sum_div of each form's projected momenta, evaluated in FP64 on
+            # that form's own links (an FP64 state loaded with them): the FP32 forms stop their
+            # projection at f32 eps * V * 320, the FP64 form at the reference's f64 eps * V * 320
+            residual = {k: [] for k in states}
+            chk = lqgpu.State(dim, L, size, beta, lqgpu.PRECISION_F64)
+            chk.set_stream(stream.cuda_stream)
             for k in range(2):
                 e_raw = rngacc.normal(0.0, 0.5 / beta, size=(L ** dim, dim, 8))
                 u = float(rngacc.uniform())
                 for name, st in states.items():
                     st.hmc_refresh_upload(e_raw)
+                    if name == "f64":
+                        residual[name].append(st.gauss_sum_div())
+                    else:
+                        chk.set_link_matrix(st.link_matrix())
+                        chk.set_e_field(st.e_field())
+                        residual[name].append(chk.gauss_sum_div())
                     p, h0, h1 = st.hmc_propose(dt, nmd)
                     st.hmc_decide(p >= 1.0 or u < p)
                     acc_out[name].append((h1 - h0, st.average_trace_plaquette().real / 3.0))
+            chk.close()
+            n_sites = L ** dim
             accuracy = {"trajectories": 2, "fp64_delta_h": [x[0] for x in acc_out["f64"]],
-                        "note": "every precision vs FP64 GPU from identical links, momenta and uniforms"}
+                        "note": "every precision vs FP64 GPU from identical links, momenta and uniforms",
+                        "fp64": {"gauss_residual": max(residual["f64"]),
+                                 "gauss_threshold": 2.220446049250313e-16 * n_sites * 320},
+                        "gauss_residual_note": "gauss_sum_div (sum over sites of |Tr((sum_a T^a) G(x))|) of the "
+                                               "projected start momenta, evaluated in FP64 on the form's own links"}
             for name in ("mixed", "f32"):
                 accuracy[name] = {
                     "max_abs_delta_h_error": max(abs(a[0] - b[0]) for a, b in zip(acc_out[name], acc_out["f64"])),
-                    "max_abs_plaquette_error": max(abs(a[1] - b[1]) for a, b in zip(acc_out[name], acc_out["f64"]))}
+                    "max_abs_plaquette_error": max(abs(a[1] - b[1]) for a, b in zip(acc_out[name], acc_out["f64"])),
+                    "gauss_residual": max(residual[name]),
+                    "gauss_threshold": 1.1920928955078125e-07 * n_sites * 320,
+                    "gauss_residual_over_fp64": max(residual[name]) / max(max(residual["f64"]), 1e-300)}
             sm.close()
             sf.close()
         so.close()

@@ -1,15 +1,14 @@
 // lq_noalloc.cu -- plaquette sums of a caller-owned device link field, with no allocation.
 //
-// Some callers cannot let a library allocate device memory: code that drives the GPU from
-// inside a CUDA-graph capture (cudaMalloc is not a capturable operation), runtimes whose
-// device memory is owned by one pool or arena (an embedding framework, a memory-capped MPS
-// client), and real-time loops for which the device-wide synchronisation implied by
-// cudaMalloc / cudaFree is not acceptable.  Every other entry point of this library keeps
-// its buffers in an lq_state, which allocates.  lq_plaquette_sums_noalloc serves those
-// callers: it reads links the caller already holds on the device and writes three sums to
-// device memory the caller provides.  Its only scratch (one partial sum per block of 128
-// sites and row) lives in the fixed array below, allocated once when the library is loaded
-// on each device and held until the process exits.
+// Some callers cannot let a library allocate device memory: runtimes whose device memory is owned by
+// one pool or arena (an embedding framework, a memory-capped MPS client), and loops for which the
+// device-wide synchronisation implied by cudaMalloc / cudaFree is not acceptable.  Every other entry
+// point of this library keeps its buffers in an lq_state, which allocates.  lq_plaquette_sums_noalloc
+// serves those callers: it reads links the caller already holds on the device and writes three sums
+// to device memory the caller provides.  Its only scratch (one partial sum per block of 128 sites and
+// row) lives in the fixed array below, allocated once when the library is loaded on each device and
+// held until the process exits.  The array's device address is looked up once per device and kept,
+// so it is not valid across a device reset.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -91,12 +90,14 @@ __global__ void __launch_bounds__(kBlock) k_plaquette_aos(const double *__restri
 #pragma unroll
         for (int mu = 0; mu < D; ++mu) {
             const uint32_t xpmu = lq::fwd(g, site, c[mu], mu);
+            // U_mu(x), once for every plane (mu, nu)
+            lq::mat3<double> umu;
+            load(site, mu, umu);
 #pragma unroll
             for (int nu = mu + 1; nu < D; ++nu) {
                 lq::mat3<double> p, q, A, B;
-                load(site, mu, p);
                 load(xpmu, nu, q);
-                lq::mul_nn(p, q, A);
+                lq::mul_nn(umu, q, A);
                 load(site, nu, p);
                 load(lq::fwd(g, site, c[nu], nu), mu, q);
                 lq::mul_nn(p, q, B);

@@ -1,8 +1,8 @@
 """The allocation-free entry point lq_plaquette_sums_noalloc, through the C ABI.
 
-It exists for callers that cannot let the library allocate device memory (inside a CUDA-graph
-capture, under a caller-owned memory pool, or in loops that cannot afford the synchronisation
-of cudaMalloc).  Its sums must equal those of the allocating entry points
+It exists for callers that cannot let the library allocate device memory (a runtime that owns all
+device memory in its own pool or arena, a memory-capped MPS client, or a loop that cannot afford the
+device-wide synchronisation of cudaMalloc / cudaFree).  Its sums must equal those of the allocating entry points
 (lq_hamiltonian_links / lq_average_trace_plaquette on an FP64 state) to the 1e-12 relative
 tolerance of the other FP64 tests, on two calls in a row that share its fixed scratch array.
 This file is collected last so a failure here comes after every other test has run.

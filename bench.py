@@ -53,8 +53,10 @@ def parse():
                     help="Gauss projection loop of the headline state: one graph launch with a device-side test "
                          "(default) or host-driven launches (profilers do not see kernels inside graphs with "
                          "conditional nodes)")
-    ap.add_argument("--batch-traj", type=int, default=10,
-                    help="timed trajectories of the batched-ensembles leg (0: skip it)")
+    ap.add_argument("--batch-traj", type=int, default=50,
+                    help="timed trajectories of the batched-ensembles leg, the configuration's 50 (0: skip it)")
+    ap.add_argument("--batch-gap-traj", type=int, default=10,
+                    help="trajectories of the batch leg's graph-gap measurement (0: skip it)")
     return ap.parse_args()
 
 
@@ -214,6 +216,39 @@ def run_reference(args):
 NCU_MD_TRAFFIC_PER_LINK = {"mixed": 994.9e6 / 2458624}
 
 
+# FP64 operations per unit of the FP64 form's kernels (D = 4): FLOP with a multiply-add as 2; the dfma,
+# dmul, dadd instruction counts per unit in parentheses are ncu's at 12^4.
+#   k_md kick+drift per link: 12 staple products, Im Tr(T^a U Sigma), two kicks, E U, the drift
+#     (1372 dfma, 157 dmul, 8 dadd); the final kick-only launch lacks E U and the drift (1272, 131, 8)
+#   k_gauss_step per link: u G u^dag and 2 Re Tr(T^a (u G u^dag) G(x+mu)) as Hermitian products, the
+#     update (175, 44, 24)
+#   k_gauss per site: D times U^dag E U as a Hermitian product, the accumulation of G and the residual
+#     (525, 146, 76.5)
+# The compiler contracts some products and sums into multiply-adds.
+FP64_FLOPS = {"md_kick_drift": 2 * 1372 + 157 + 8, "md_kick": 2 * 1272 + 131 + 8,
+              "gauss_step": 2 * 175 + 44 + 24, "gauss": 2 * 525 + 146 + 76.5}
+
+
+def fp64_roofline(prof64, n_links, n_sites, md_steps, trajectories, peak):
+    """achieved FP64 FLOP/s of the FP64 form's kernel classes over the timed trajectories, against the
+    measured multiply-add peak (lq_fma_peak): those kernels are bound by the FP64 pipe, not by HBM"""
+    md_n, md_ms = prof64["md"]
+    st_n, st_ms = prof64["gauss_sweep"]  # the FP64 projection's step launches
+    ga_n, ga_ms = prof64["gauss"]
+    md_flops = n_links * (md_steps * FP64_FLOPS["md_kick_drift"] + FP64_FLOPS["md_kick"]) * trajectories
+    out = {"peak_tflops": peak / 1e12, "peak_kind": "measured: lq_fma_peak, FP64 multiply-add chains on every SM",
+           "flop_counts": "ncu FP64 instruction counts at 12^4 (2 FLOP per dfma), per link or site: " +
+                          json.dumps(FP64_FLOPS)}
+    for name, flops, ms, n in (("k_md", md_flops, md_ms, md_n),
+                               ("k_gauss_step", st_n * n_links * FP64_FLOPS["gauss_step"], st_ms, st_n),
+                               ("k_gauss", ga_n * n_sites * FP64_FLOPS["gauss"], ga_ms, ga_n)):
+        if ms > 0 and n > 0:
+            achieved = flops / (ms / 1000.0)
+            out[name] = {"launches": n, "ms_per_launch": ms / n, "achieved_tflops": achieved / 1e12,
+                         "frac": achieved / peak}
+    return out
+
+
 def algorithmic_md_bytes(n_links, md_steps, real_bytes, compensated=False):
     """Bytes moved by the fused MD kernels of one trajectory at ideal neighbour reuse.
     kick+drift launch: read U (18 reals) + E (8) + write E (8) + U' (18) = 52 reals per link;
@@ -292,6 +327,7 @@ def batch_leg(args, stream, peak):
     ms = ev0.elapsed_time(ev1)
     r = b.hmc_results()
     launches = b.graph_launches() - launches0
+    gap = batch_graph_gap(b, stream, dt, nmd, args.batch_gap_traj, 3 + args.batch_traj) if args.batch_gap_traj else None
     b.close()
     md_bytes = links * 52 * 8
     ok = r["status"] == 0
@@ -311,7 +347,44 @@ def batch_leg(args, stream, peak):
             "projection_failure_cause": "NaN residual (LQ_ERR_GAUSS_PROJECTION): the reference's projection step is "
                                         "quadratic in the Gauss law and diverges for momenta of standard deviation "
                                         "0.5/beta near 1; the ensemble keeps its links",
-            "acceptance": float(r["accepted"][ok].mean()) if ok.any() else None}
+            "acceptance": float(r["accepted"][ok].mean()) if ok.any() else None,
+            "graph_gap": gap}
+
+
+def batch_graph_gap(b, stream, dt, nmd, n_traj, counter):
+    """The graph's cost between its kernel nodes: the same n_traj trajectories (links and Philox
+    counters restored in between, results checked equal) run once as graph launches, timed by CUDA
+    events around them, and once as eager launches with every kernel bracketed by CUDA events
+    (lq_batch_profile_*); gap = 1 - summed kernel time / graph time."""
+    import numpy as np
+    import torch
+
+    links = [b.link_matrix(e) for e in range(b.n)]
+    b.set_seed(3, counter)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    b.hmc_run(dt, nmd, n_traj)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = ev0.elapsed_time(ev1)
+    rg = b.hmc_results()
+    for e, x in enumerate(links):
+        b.set_link_matrix(e, x)
+    b.set_seed(3, counter)
+    b.profile_enable(True)
+    b.profile_read(reset=True)
+    b.hmc_run(dt, nmd, n_traj, graph=False)
+    n_kernels, kernel_ms = b.profile_read(reset=True)
+    b.profile_enable(False)
+    re_ = b.hmc_results()
+    # failed projections record NaN: equal NaNs count as equal
+    same = all(np.array_equal(rg[k], re_[k], equal_nan=(k == "delta_h")) for k in ("delta_h", "accepted", "gauss_steps"))
+    return {"trajectories": n_traj, "graph_ms_per_trajectory": graph_ms / n_traj,
+            "kernel_ms_per_trajectory": kernel_ms / n_traj, "kernels_per_trajectory": n_kernels / n_traj,
+            "gap_fraction": 1.0 - kernel_ms / graph_ms, "same_results": bool(same),
+            "method": "the same trajectories (links and counters restored) as graph launches timed by events around "
+                      "them and as eager launches with an event pair around every kernel"}
 
 
 def run_ours(args):
@@ -423,7 +496,10 @@ def run_ours(args):
                "h2d_bytes_per_step": int(np.prod(shape) * 8), "d2h_bytes_per_step": int(d2h / args.e2e_steps),
                "path": "lq_efield_prefetch + lq_hmc_refresh_prefetched + lq_hmc_propose + lq_hmc_decide + "
                        "lq_average_trace_plaquette, momenta (f64, reference layout) from pinned host memory each "
-                       "trajectory, the next trajectory's copy overlapping the current one"}
+                       "trajectory, the next trajectory's copy overlapping the current one",
+               "scope": "the C ABI called from Python (ctypes) as the reference's HMC driver would call it; the "
+                        "links stay resident on the device (the state is device-resident), only the momenta and "
+                        "the scalar results cross the bus"}
     plaq_mixed = s.average_trace_plaquette()
     s.close()
 
@@ -443,7 +519,10 @@ def run_ours(args):
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.fp64_steps,
                 "headline_over_fp64": value / v64,
                 "md_kernel_ms": md64_ms / max(1, md64_n),
-                "gauss_steps": [r["gauss_steps"] for r in res64]}
+                "gauss_steps": [r["gauss_steps"] for r in res64],
+                "kernel_ms": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof64.items()},
+                "roofline_fp64": fp64_roofline(prof64, n_links, L ** dim, nmd, args.fp64_steps,
+                                               lqgpu.fma_peak(lqgpu.PRECISION_F64))}
         other = lqgpu.PRECISION_F32 if prec == lqgpu.PRECISION_MIXED else lqgpu.PRECISION_MIXED
         so = lqgpu.State(dim, L, size, beta, other)
         so.set_stream(stream.cuda_stream)

@@ -101,6 +101,21 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
 int lq_state_destroy(lq_state *s);
 /* Clone for State: Clone (src/simulation/monte_carlo/hybrid_monte_carlo.rs:318); same stream. */
 int lq_state_clone(const lq_state *s, lq_state **out);
+/* Whole-state checkpoint: the serde derives of LatticeStateDefault / LatticeStateEFSyncDefault
+ * (src/simulation/state.rs:653-654, :1046-1047) serialise the lattice, beta, the links, the E-field
+ * and t.  lq_state_save writes all of it into a host buffer of lq_state_checkpoint_bytes bytes: a
+ * 112-byte little-endian header (magic "LQGPUCK1", version, D, L, precision, size, beta, t, the
+ * leap-frog flag, the link update and the projection-loop choice), then the device's link and
+ * E-field arrays as stored, compensated lo halves included, so lq_state_load gives a state that
+ * continues bitwise as the saved one would (the HMC random streams are the caller's seed and
+ * counter).  The image is this library's own format; the serde layouts stay available through
+ * lq_links_download / lq_efield_download.  Saving with an undecided HMC proposal returns
+ * LQ_ERR_INVALID_ARGUMENT; a buffer of the wrong size LQ_ERR_INCOMPATIBLE_SIZE; lq_state_load
+ * rejects a buffer without the magic and version with LQ_ERR_INVALID_ARGUMENT.  The loaded state
+ * uses the legacy default stream. */
+int lq_state_checkpoint_bytes(const lq_state *s, size_t *bytes);
+int lq_state_save(lq_state *s, void *buf, size_t n_bytes);
+int lq_state_load(const void *buf, size_t n_bytes, lq_state **out);
 /* Attach a cudaStream_t (passed as void*); NULL selects the legacy default stream. */
 int lq_state_set_stream(lq_state *s, void *cuda_stream);
 /* The Gauss projection's sweep loop (EField::project_to_gauss, src/field.rs:1265-1294) of the
@@ -109,7 +124,7 @@ int lq_state_set_stream(lq_state *s, void *cuda_stream);
  * one host read of the residual per test (enable = 0).  Both give the same sweeps and the same
  * field; the FP64 form always uses host-driven launches.  A driver that cannot build the graph
  * turns it off for the state.  Without a step limit (max_steps <= 0) the graph's device-side loop
- * still stops after 2^20 sweeps with LQ_ERR_NOT_CONVERGED. */
+ * still stops after 10001 sweeps with LQ_ERR_NOT_CONVERGED, the limit of a batch's loop too. */
 int lq_state_set_projection_graph(lq_state *s, int enable);
 /* Getters: LatticeCyclic::dim/size, LatticeState::beta, LatticeStateWithEField::t,
  * number_of_points (src/lattice.rs:208-233). is_leap = 1 between sync_leap and leap_sync. */
@@ -292,16 +307,21 @@ enum lq_kernel_class {
     LQ_KERNEL_CLASSES = 6
 };
 int lq_profile_enable(lq_state *s, int on);
+/* Measured multiply-add peak of the current device (no reference counterpart): long chains of
+ * independent multiply-adds in LQ_PRECISION_F64 or LQ_PRECISION_F32 on every SM, timed with CUDA
+ * events at the clocks the device runs at; *flops_per_s counts 2 FLOP per multiply-add.  The
+ * denominator of the compute roofline of the FP64 form, whose kernels the FP64 pipe bounds. */
+int lq_fma_peak(int precision, double *flops_per_s);
 /* launches and total milliseconds of one class since the last reset; also resets when reset != 0 */
 int lq_profile_read(lq_state *s, int kernel_class, long long *launches, double *total_ms, int reset);
 
 /* ---------------------------------------------------------------- without allocation
  * No counterpart in the reference.  For callers that cannot let this library allocate device
- * memory -- code running inside a CUDA-graph capture (cudaMalloc cannot be captured), code
- * whose device memory belongs to one pool or arena (an embedding framework, a memory-capped
- * MPS client), and loops that cannot afford the device-wide synchronisation of cudaMalloc /
- * cudaFree.  Computes the plaquette sums of links the caller holds on the device in the serde
- * layout (double[L^dim * dim][18]) and writes them to d_out[0..2] on the device:
+ * memory: a runtime whose device memory belongs to one pool or arena it manages itself (an
+ * embedding framework, a memory-capped MPS client), or a loop that cannot afford the device-wide
+ * synchronisation of cudaMalloc / cudaFree.  Computes the plaquette sums of links the caller holds
+ * on the device in the serde layout (double[L^dim * dim][18]) and writes them to d_out[0..2] on the
+ * device:
  *   d_out[0] = sum (1 - Re Tr P / 3)   (hamiltonian_links = beta * d_out[0])
  *   d_out[1] = sum Re Tr P, d_out[2] = sum Im Tr P
  *              (average_trace_plaquette = (d_out[1] + i d_out[2]) / (L^dim * dim (dim-1) / 2)).
@@ -311,8 +331,9 @@ int lq_profile_read(lq_state *s, int kernel_class, long long *launches, double *
  * 1.5 MiB device array that every device loading the library holds until the process exits;
  * all calls share it, so calls whose work overlaps on the GPU (other streams, other host
  * threads) race and must be serialised by the caller.  The first call on a device looks up the
- * array's device address with that device current; make that first call before any stream
- * capture. */
+ * array's device address with that device current and keeps it for the process; make that first
+ * call before any stream capture, and do not use the entry point across a device reset
+ * (cudaDeviceReset), after which the kept address is stale. */
 int lq_plaquette_sums_noalloc(int dim, int L, const double *d_links, double *d_out, void *stream);
 
 /* ---------------------------------------------------------------- batched ensembles
@@ -384,6 +405,13 @@ int lq_batch_hmc_results(lq_batch *b, int first, int count, double *delta_h, dou
                          int *accepted, int *gauss_steps, int *status, double *plaquette);
 /* graph launches since creation */
 int lq_batch_graph_launches(const lq_batch *b, long long *launches);
+/* Kernel time of eagerly launched trajectories (no reference counterpart): while enabled, every
+ * launch of an lq_batch_hmc_run without LQ_BATCH_USE_GRAPH is bracketed by a CUDA event pair on the
+ * batch's stream; lq_batch_profile_read returns the launches and their summed milliseconds since
+ * the last reset.  Launches inside the captured graph are never bracketed: comparing this sum with
+ * the graph's own time on the same trajectories measures the graph's gaps between nodes. */
+int lq_batch_profile_enable(lq_batch *b, int on);
+int lq_batch_profile_read(lq_batch *b, long long *launches, double *kernel_ms, int reset);
 
 /* ---------------------------------------------------------------- diagnostics */
 const char *lq_status_string(int status);

@@ -118,6 +118,16 @@ struct Batch {
     int g_steps = 0, g_max_gauss = 0, g_flags = 0, g_link_update = -1;
     long long graph_launches = 0;
 
+    // kernel time of eagerly launched trajectories (lq_batch_profile_enable): an event pair around
+    // every launch, summed at each synchronisation; never inside a capture
+    static constexpr int kProfPairs = 512;
+    int prof_on = 0;
+    int capturing = 0;
+    cudaEvent_t *prof_ev = nullptr; // 2 * kProfPairs events while profiling is enabled
+    int prof_n = 0;
+    long long prof_launches = 0;
+    double prof_ms = 0.0;
+
     const BatchOps *ops = nullptr;
 
     size_t link_elems() const { return (size_t)total_tiles * 32 * dim * 9; }

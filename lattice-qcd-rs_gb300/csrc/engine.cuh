@@ -215,6 +215,9 @@ template <int D, typename T, bool COMP> struct Engine {
     // Metropolis partials (2 rows) in s.partial, their count in *n_partials
     static cudaError_t mc_sweep(State &s, void *U, int alg, int mu, int parity, double beta, uint64_t seed,
                                 uint64_t sweep, int n_update, double spread, uint32_t *n_partials) {
+        // k_mc_sweep maps thread t to row 2t / L and there to the sites of the class's parity along
+        // x0: valid for even L only (every caller checks this too; an odd L never reaches a launch)
+        if (s.L % 2 != 0) return cudaErrorInvalidValue;
         const uint32_t blocks = (s.V / 2 + 127) / 128; // one thread per site of the class
         const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
 #define LQ_MC_CASE(A)                                                                                                  \

@@ -315,13 +315,9 @@ int capture_projection(State &s, int max_steps, cudaGraphExec_t *out) {
     return LQ_OK;
 }
 
-// A step limit for the graph's device-side loop when the caller sets none (max_steps <= 0): the
-// loop always ends (after 2^20 sweeps, several minutes at 32^4, with LQ_ERR_NOT_CONVERGED).
-constexpr int kProjGraphMaxSweeps = 1 << 20;
-
 // project_gauss through the captured graph: one launch and one read of (sweeps, status)
 int project_gauss_graph(State &s, int max_steps, int *steps_done) {
-    if (max_steps <= 0) max_steps = kProjGraphMaxSweeps;
+    if (max_steps <= 0) max_steps = lq::kDefaultProjectionSteps;
     const void *U = s.U[s.cur];
     cudaGraphExec_t exec = nullptr;
     for (int i = 0; i < s.n_proj; ++i) {
@@ -549,10 +545,106 @@ int lq_state_clone(const lq_state *src, lq_state **out) {
     }
     c->t = src->t;
     c->leap = src->leap;
+    c->link_update = src->link_update;
     c->proj_graph = src->proj_graph;
     c->hu_valid = src->hu_valid;
     c->hu = src->hu;
     *out = c;
+    return LQ_OK;
+}
+
+// ---- whole-state checkpoint: a little-endian header, then the raw device fields
+namespace {
+constexpr char kCheckpointMagic[8] = {'L', 'Q', 'G', 'P', 'U', 'C', 'K', '1'};
+constexpr uint32_t kCheckpointVersion = 1;
+struct CheckpointHeader {
+    char magic[8];
+    uint32_t version;
+    int32_t dim, L, precision;
+    double size, beta;
+    int64_t t;
+    int32_t leap, link_update, proj_graph, reserved0;
+    uint64_t link_bytes, efield_bytes;
+    uint64_t reserved[4];
+};
+static_assert(sizeof(CheckpointHeader) == 112, "checkpoint header layout");
+} // namespace
+
+int lq_state_checkpoint_bytes(const lq_state *s, size_t *bytes) {
+    LQ_CHECK_STATE(s);
+    if (!bytes) return LQ_ERR_INVALID_ARGUMENT;
+    *bytes = sizeof(CheckpointHeader) + s->link_bytes() + s->efield_bytes();
+    return LQ_OK;
+}
+
+int lq_state_save(lq_state *s, void *buf, size_t n_bytes) {
+    LQ_CHECK_STATE(s);
+    if (!buf) return LQ_ERR_INVALID_ARGUMENT;
+    if (n_bytes != sizeof(CheckpointHeader) + s->link_bytes() + s->efield_bytes()) return LQ_ERR_INCOMPATIBLE_SIZE;
+    if (s->has_pending) {
+        g_last_error = "lq_state_save: an HMC proposal is pending (lq_hmc_decide first)";
+        return LQ_ERR_INVALID_ARGUMENT;
+    }
+    CheckpointHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, kCheckpointMagic, sizeof(h.magic));
+    h.version = kCheckpointVersion;
+    h.dim = s->dim;
+    h.L = s->L;
+    h.precision = s->precision;
+    h.size = s->size;
+    h.beta = s->beta;
+    h.t = s->t;
+    h.leap = s->leap;
+    h.link_update = s->link_update;
+    h.proj_graph = s->proj_graph;
+    h.link_bytes = s->link_bytes();
+    h.efield_bytes = s->efield_bytes();
+    char *dst = static_cast<char *>(buf);
+    memcpy(dst, &h, sizeof(h));
+    LQ_CK(cudaMemcpyAsync(dst + sizeof(h), s->U[s->cur], h.link_bytes, cudaMemcpyDeviceToHost, s->stream));
+    LQ_CK(cudaMemcpyAsync(dst + sizeof(h) + h.link_bytes, s->E, h.efield_bytes, cudaMemcpyDeviceToHost, s->stream));
+    LQ_CK(sync_stream(*s));
+    return LQ_OK;
+}
+
+int lq_state_load(const void *buf, size_t n_bytes, lq_state **out) {
+    if (!buf || !out) return LQ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    CheckpointHeader h;
+    if (n_bytes < sizeof(h)) return LQ_ERR_INCOMPATIBLE_SIZE;
+    memcpy(&h, buf, sizeof(h));
+    if (memcmp(h.magic, kCheckpointMagic, sizeof(h.magic)) != 0 || h.version != kCheckpointVersion) {
+        g_last_error = "lq_state_load: not a checkpoint of this library (magic or version)";
+        return LQ_ERR_INVALID_ARGUMENT;
+    }
+    if (n_bytes != sizeof(h) + h.link_bytes + h.efield_bytes) return LQ_ERR_INCOMPATIBLE_SIZE;
+    if (h.leap != 0 && h.leap != 1) return LQ_ERR_INVALID_ARGUMENT;
+    if (h.link_update < LQ_LINK_UPDATE_EULER || h.link_update > LQ_LINK_UPDATE_EXP_REUNITARIZE)
+        return LQ_ERR_INVALID_ARGUMENT;
+    lq_state *s = nullptr;
+    int rc = lq_state_create(h.dim, h.L, h.size, h.beta, h.precision, &s);
+    if (rc) return rc;
+    if (s->link_bytes() != h.link_bytes || s->efield_bytes() != h.efield_bytes) {
+        free_state(s);
+        return LQ_ERR_INCOMPATIBLE_SIZE;
+    }
+    const char *src = static_cast<const char *>(buf) + sizeof(h);
+    cudaError_t e = cudaMemcpyAsync(s->U[0], src, h.link_bytes, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->E, src + h.link_bytes, h.efield_bytes, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "checkpoint load", __LINE__);
+        free_state(s);
+        return rc;
+    }
+    s->cur = 0;
+    s->t = h.t;
+    s->leap = h.leap;
+    s->link_update = h.link_update;
+    s->proj_graph = h.proj_graph ? 1 : 0;
+    *out = s;
     return LQ_OK;
 }
 

@@ -18,6 +18,7 @@
 #include "batch.hpp"
 #include "kernels.cuh"
 #include "lqgpu.h"
+#include "state.hpp"
 
 using lq::Batch;
 
@@ -41,9 +42,6 @@ __global__ void __launch_bounds__(256) k_batch_setup(uint64_t *keys, BatchRun *r
 
 namespace {
 
-// the device loop of the projection needs a bound when the caller gives none
-constexpr int kDefaultMaxGaussSteps = 10001;
-
 int bfail(cudaError_t e, const char *what, int line) {
     char buf[512];
     snprintf(buf, sizeof(buf), "%s (%s) in %s at lq_batch.cu:%d", cudaGetErrorName(e), cudaGetErrorString(e), what,
@@ -58,6 +56,50 @@ int bfail(cudaError_t e, const char *what, int line) {
 #define BK(call)                                                                                                       \
     do {                                                                                                               \
         cudaError_t _e = (call);                                                                                       \
+        if (_e != cudaSuccess) return bfail(_e, #call, __LINE__);                                                      \
+    } while (0)
+
+// ---- kernel timing of eager trajectories
+void bprof_flush(Batch &b) {
+    for (int i = 0; i < b.prof_n; ++i) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, b.prof_ev[2 * i], b.prof_ev[2 * i + 1]) == cudaSuccess) {
+            b.prof_ms += ms;
+            ++b.prof_launches;
+        } else {
+            (void)cudaGetLastError();
+        }
+    }
+    b.prof_n = 0;
+}
+int bprof_begin(Batch &b) {
+    if (!b.prof_on || b.capturing || !b.prof_ev) return -1;
+    if (b.prof_n == Batch::kProfPairs) {
+        if (cudaStreamSynchronize(b.stream) != cudaSuccess) return -1;
+        bprof_flush(b);
+    }
+    cudaEventRecord(b.prof_ev[2 * b.prof_n], b.stream);
+    return b.prof_n;
+}
+void bprof_end(Batch &b, int slot) {
+    if (slot < 0) return;
+    cudaEventRecord(b.prof_ev[2 * slot + 1], b.stream);
+    b.prof_n = slot + 1;
+}
+void bprof_free(Batch &b) {
+    if (!b.prof_ev) return;
+    for (int i = 0; i < 2 * Batch::kProfPairs; ++i) cudaEventDestroy(b.prof_ev[i]);
+    delete[] b.prof_ev;
+    b.prof_ev = nullptr;
+    b.prof_on = 0;
+}
+
+// a launch of the trajectory, timed while profiling eager trajectories
+#define BKL(call)                                                                                                      \
+    do {                                                                                                               \
+        const int _slot = bprof_begin(b);                                                                              \
+        cudaError_t _e = (call);                                                                                       \
+        bprof_end(b, _slot);                                                                                           \
         if (_e != cudaSuccess) return bfail(_e, #call, __LINE__);                                                      \
     } while (0)
 
@@ -84,6 +126,7 @@ void drop_graph(Batch &b) {
 void free_batch(Batch *b) {
     if (!b) return;
     drop_graph(*b);
+    bprof_free(*b);
     for (int i = 0; i < 3; ++i)
         if (b->U[i]) cudaFree(b->U[i]);
     for (int i = 0; i < 2; ++i) {
@@ -156,18 +199,18 @@ int state_buffer(Batch &b, int e, int *buf) {
 // momenta; the projected start momenta end in E[1] (every ensemble stops after 1, 5, 9, ...
 // sweeps and is skipped in between, so all of them finish in E[1]).
 int enqueue_projection_start(Batch &b, int max_steps, cudaGraphConditionalHandle h, int use_handle) {
-    BK(b.ops->normal(b, 0));
-    BK(b.ops->gauss(b, 0, 0));
-    BK(b.ops->sweep(b, 0, 1, 0, 1));
-    BK(b.ops->check(b, 1, max_steps, h, use_handle));
+    BKL(b.ops->normal(b, 0));
+    BKL(b.ops->gauss(b, 0, 0));
+    BKL(b.ops->sweep(b, 0, 1, 0, 1));
+    BKL(b.ops->check(b, 1, max_steps, h, use_handle));
     return LQ_OK;
 }
 int enqueue_projection_block(Batch &b, int max_steps, cudaGraphConditionalHandle h, int use_handle) {
-    BK(b.ops->sweep(b, 1, 0, 1, 0));
-    BK(b.ops->sweep(b, 0, 1, 0, 1));
-    BK(b.ops->sweep(b, 1, 0, 1, 0));
-    BK(b.ops->sweep(b, 0, 1, 0, 1));
-    BK(b.ops->check(b, 4, max_steps, h, use_handle));
+    BKL(b.ops->sweep(b, 1, 0, 1, 0));
+    BKL(b.ops->sweep(b, 0, 1, 0, 1));
+    BKL(b.ops->sweep(b, 1, 0, 1, 0));
+    BKL(b.ops->sweep(b, 0, 1, 0, 1));
+    BKL(b.ops->check(b, 4, max_steps, h, use_handle));
     return LQ_OK;
 }
 // leap-frog from the state (role 0) with momenta E[1] -> E[0], Delta H, accept
@@ -175,24 +218,24 @@ int enqueue_md_accept(Batch &b, double dt, int n, int flags) {
     if (b.comp) {
         // the sweeps updated the hi parts only: the projected field is hi + 0
         const size_t half = b.efield_bytes() / 2;
-        BK(cudaMemsetAsync((char *)b.E[1] + half, 0, half, b.stream));
+        BKL(cudaMemsetAsync((char *)b.E[1] + half, 0, half, b.stream));
     }
     // the coefficients of dt are in the ensemble table (set_step_coefficients)
     (void)dt;
     const int KD = lq::MD_KICK | lq::MD_DRIFT | link_update_bits(b.link_update);
-    BK(b.ops->md(b, 0, 1, 1, 0, KD, 0));
+    BKL(b.ops->md(b, 0, 1, 1, 0, KD, 0));
     int cur = 1, nxt = 2;
     for (int i = 1; i < n; ++i) {
-        BK(b.ops->md(b, cur, nxt, 0, 0, KD, 1));
+        BKL(b.ops->md(b, cur, nxt, 0, 0, KD, 1));
         const int t = cur;
         cur = nxt;
         nxt = t;
     }
-    BK(b.ops->md(b, cur, cur, 0, 0, lq::MD_KICK, 0));
-    BK(b.ops->plaquette_delta(b, 0, cur));
-    BK(b.ops->sumsq_delta(b, 1, 0));
-    BK(b.ops->accept(b, cur));
-    if (flags & LQ_BATCH_MEASURE_PLAQUETTE) BK(b.ops->record_plaquette(b));
+    BKL(b.ops->md(b, cur, cur, 0, 0, lq::MD_KICK, 0));
+    BKL(b.ops->plaquette_delta(b, 0, cur));
+    BKL(b.ops->sumsq_delta(b, 1, 0));
+    BKL(b.ops->accept(b, cur));
+    if (flags & LQ_BATCH_MEASURE_PLAQUETTE) BKL(b.ops->record_plaquette(b));
     return LQ_OK;
 }
 
@@ -209,7 +252,15 @@ int run_eager(Batch &b, double dt, int n, int max_steps, int flags) {
     return enqueue_md_accept(b, dt, n, flags);
 }
 
+int capture_inner(Batch &b, double dt, int n, int max_steps, int flags);
 int capture(Batch &b, double dt, int n, int max_steps, int flags) {
+    // no event records inside the captured graph
+    b.capturing = 1;
+    const int rc = capture_inner(b, dt, n, max_steps, flags);
+    b.capturing = 0;
+    return rc;
+}
+int capture_inner(Batch &b, double dt, int n, int max_steps, int flags) {
     drop_graph(b);
     BK(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
     cudaGraph_t g = nullptr;
@@ -634,7 +685,7 @@ int lq_batch_hmc_run(lq_batch *b, double dt, int n_steps, int n_trajectories, in
     if (n_steps <= 0) return LQ_ERR_ZERO_INTEGRATION;
     if (n_trajectories <= 0 || (flags & ~(LQ_BATCH_USE_GRAPH | LQ_BATCH_MEASURE_PLAQUETTE)))
         return LQ_ERR_INVALID_ARGUMENT;
-    const int max_steps = max_gauss_steps > 0 ? max_gauss_steps : kDefaultMaxGaussSteps;
+    const int max_steps = max_gauss_steps > 0 ? max_gauss_steps : lq::kDefaultProjectionSteps;
     int rc = ensure_results(*b, n_trajectories);
     if (!rc) rc = set_step_coefficients(*b, dt);
     if (rc) return rc;
@@ -678,6 +729,43 @@ int lq_batch_hmc_results(lq_batch *b, int first, int count, double *delta_h, dou
         if (gauss_steps) gauss_steps[i] = r.gauss_steps;
         if (status) status[i] = r.status;
         if (plaquette) plaquette[i] = r.plaq_re;
+    }
+    return LQ_OK;
+}
+
+int lq_batch_profile_enable(lq_batch *b, int on) {
+    BCHECK(b);
+    if (on && !b->prof_ev) {
+        b->prof_ev = new (std::nothrow) cudaEvent_t[2 * Batch::kProfPairs];
+        if (!b->prof_ev) return LQ_ERR_OUT_OF_MEMORY;
+        for (int i = 0; i < 2 * Batch::kProfPairs; ++i) {
+            const cudaError_t e = cudaEventCreate(&b->prof_ev[i]);
+            if (e != cudaSuccess) {
+                for (int j = 0; j < i; ++j) cudaEventDestroy(b->prof_ev[j]);
+                delete[] b->prof_ev;
+                b->prof_ev = nullptr;
+                return bfail(e, "cudaEventCreate", __LINE__);
+            }
+        }
+    }
+    if (!on) {
+        BK(cudaStreamSynchronize(b->stream));
+        bprof_flush(*b);
+        bprof_free(*b);
+    }
+    b->prof_on = on ? 1 : 0;
+    return LQ_OK;
+}
+
+int lq_batch_profile_read(lq_batch *b, long long *launches, double *kernel_ms, int reset) {
+    BCHECK(b);
+    BK(cudaStreamSynchronize(b->stream));
+    if (b->prof_ev) bprof_flush(*b);
+    if (launches) *launches = b->prof_launches;
+    if (kernel_ms) *kernel_ms = b->prof_ms;
+    if (reset) {
+        b->prof_launches = 0;
+        b->prof_ms = 0.0;
     }
     return LQ_OK;
 }

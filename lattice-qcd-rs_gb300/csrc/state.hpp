@@ -156,6 +156,11 @@ const Ops *ops_f64(int dim);
 const Ops *ops_f32(int dim);
 const Ops *ops_mixed(int dim);
 
+// Step limit of every device-side projection loop (a single state's graph, a batch's) when the
+// caller gives none (max_steps <= 0): 1 + 4 * 2500 sweeps, the reference's schedule, so the loop
+// always ends (LQ_ERR_NOT_CONVERGED); at 32^4 about 1.4 s of FP32 sweeps.
+constexpr int kDefaultProjectionSteps = 10001;
+
 // partial slots needed for V sites (per row), and the rows of the partial buffer
 inline uint32_t partial_slots_for(uint32_t V) { return (V + 127) / 128 + 64; }
 constexpr int kPartialRows = 3;

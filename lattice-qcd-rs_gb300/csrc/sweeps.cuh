@@ -435,9 +435,10 @@ template <int D, typename T, bool COMP, int ALG>
 __global__ void __launch_bounds__(128) k_mc_sweep(V2<T> *__restrict__ U, Geo<D> g, int mu, int parity, double beta,
                                                   uint2 key, uint32_t s_lo, uint32_t s_hi, int n_update,
                                                   double spread, double *__restrict__ partial) {
-    // one thread per site of the class (L is even): thread t takes row r = 2t / L (the sites with
-    // x1.. fixed) and there the j-th site, j = t - r L / 2, whose coordinate sum has the class's
-    // parity, so every lane of a warp has a link to update
+    // one thread per site of the class: thread t takes row r = 2t / L (the sites with x1.. fixed)
+    // and there the j-th site, j = t - r L / 2, whose coordinate sum has the class's parity, so every
+    // lane of a warp has a link to update.  Preconditions, checked by the launcher: L even (each row
+    // then holds L / 2 sites of either parity) and x0 the fastest coordinate of the site index.
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     double v[2] = {0.0, 0.0};
     uint32_t c[D];

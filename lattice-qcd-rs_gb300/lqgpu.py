@@ -47,6 +47,9 @@ SIGNATURES = {
     "lq_state_create": (_i32, [_i32, _i32, _f64, _f64, _i32, ctypes.POINTER(_vp)]),
     "lq_state_destroy": (_i32, [_vp]),
     "lq_state_clone": (_i32, [_vp, ctypes.POINTER(_vp)]),
+    "lq_state_checkpoint_bytes": (_i32, [_vp, _szp]),
+    "lq_state_save": (_i32, [_vp, _vp, _sz]),
+    "lq_state_load": (_i32, [_vp, _sz, ctypes.POINTER(_vp)]),
     "lq_state_set_stream": (_i32, [_vp, _vp]),
     "lq_state_set_projection_graph": (_i32, [_vp, _i32]),
     "lq_state_info": (_i32, [_vp, _ip, _ip, _dp, _dp, _ip, _llp, _llp, _ip]),
@@ -90,6 +93,7 @@ SIGNATURES = {
     "lq_leapfrog_adjoint": (_i32, [_vp, _f64, _i32, _i32, _dp, _dp, _dp, _sz, _dp, _sz, _szp]),
     "lq_profile_enable": (_i32, [_vp, _i32]),
     "lq_profile_read": (_i32, [_vp, _i32, _llp, _dp, _i32]),
+    "lq_fma_peak": (_i32, [_i32, _dp]),
     "lq_batch_create": (_i32, [_i32, _i32, _ip, _dp, _dp, _i32, ctypes.POINTER(_vp)]),
     "lq_batch_destroy": (_i32, [_vp]),
     "lq_batch_set_stream": (_i32, [_vp, _vp]),
@@ -106,6 +110,8 @@ SIGNATURES = {
     "lq_batch_hmc_run": (_i32, [_vp, _f64, _i32, _i32, _i32, _i32]),
     "lq_batch_hmc_results": (_i32, [_vp, _i32, _i32, _dp, _dp, _dp, _ip, _ip, _ip, _dp]),
     "lq_batch_graph_launches": (_i32, [_vp, _llp]),
+    "lq_batch_profile_enable": (_i32, [_vp, _i32]),
+    "lq_batch_profile_read": (_i32, [_vp, _llp, _dp, _i32]),
     "lq_status_string": (ctypes.c_char_p, [_i32]),
     "lq_last_error_string": (ctypes.c_char_p, []),
     "lq_version": (_i32, []),
@@ -188,6 +194,28 @@ class State:
         h = _vp()
         _check(load().lq_state_clone(self._h, ctypes.byref(h)), "lq_state_clone")
         return State(self.dim, self.L, self.size, self.beta, self.precision, _handle=h)
+
+    def save(self):
+        """the whole state as a checkpoint image (bytes): header, then the device fields as stored"""
+        n = ctypes.c_size_t()
+        _check(load().lq_state_checkpoint_bytes(self._h, ctypes.byref(n)), "lq_state_checkpoint_bytes")
+        buf = ctypes.create_string_buffer(n.value)
+        _check(load().lq_state_save(self._h, buf, n.value), "lq_state_save")
+        return buf.raw
+
+    @classmethod
+    def load(cls, image):
+        """a new state from a checkpoint image of State.save"""
+        image = bytes(image)
+        h = _vp()
+        _check(load().lq_state_load(image, len(image), ctypes.byref(h)), "lq_state_load")
+        s = cls.__new__(cls)
+        s._h = h
+        info = s.info()
+        s.dim, s.L, s.size, s.precision = info["dim"], info["L"], info["size"], info["precision"]
+        s.n_sites = s.L ** s.dim
+        s.n_links = s.n_sites * s.dim
+        return s
 
     def set_stream(self, stream_ptr):
         _check(load().lq_state_set_stream(self._h, _vp(stream_ptr)), "lq_state_set_stream")
@@ -521,7 +549,25 @@ class Batch:
         return dict(delta_h=dh, prob=p, uniform=u, accepted=acc.astype(bool), gauss_steps=steps, status=st,
                     plaquette=pl)
 
+    def profile_enable(self, on=True):
+        """time every launch of eager trajectories (hmc_run(graph=False)) with CUDA events"""
+        _check(load().lq_batch_profile_enable(self._h, 1 if on else 0), "lq_batch_profile_enable")
+
+    def profile_read(self, reset=False):
+        """(launches, summed kernel milliseconds) of eager trajectories since the last reset"""
+        n, ms = ctypes.c_longlong(), ctypes.c_double()
+        _check(load().lq_batch_profile_read(self._h, ctypes.byref(n), ctypes.byref(ms), 1 if reset else 0),
+               "lq_batch_profile_read")
+        return n.value, ms.value
+
     def graph_launches(self):
         n = ctypes.c_longlong()
         _check(load().lq_batch_graph_launches(self._h, ctypes.byref(n)), "lq_batch_graph_launches")
         return n.value
+
+
+def fma_peak(precision=PRECISION_F64):
+    """measured multiply-add peak of the current device in FLOP/s (lq_fma_peak)"""
+    v = ctypes.c_double()
+    _check(load().lq_fma_peak(precision, ctypes.byref(v)), "lq_fma_peak")
+    return v.value

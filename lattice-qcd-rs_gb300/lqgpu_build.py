@@ -20,7 +20,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
 ]
-SOURCES = ["lq_api.cu", "lq_f64.cu", "lq_f32.cu", "lq_mixed.cu", "lq_noalloc.cu", "lq_batch.cu",
+SOURCES = ["lq_api.cu", "lq_f64.cu", "lq_f32.cu", "lq_mixed.cu", "lq_noalloc.cu", "lq_peak.cu", "lq_batch.cu",
            "lq_batch_f64.cu", "lq_batch_f32.cu", "lq_batch_mixed.cu"]
 
 

@@ -28,8 +28,13 @@ distribution: HMC and checkerboard Metropolis on the same lattice and beta give 
 
 tour      : every kernel once at 32^4 (for a per-kernel ncu launch list with DRAM bytes).
 
-usage: python studies.py precision [--traj N] [--size L] | scale [--traj K] [--size L] | tour [--L 32] | batch [--traj N] | adjoint [--L 48]
-       | distribution [--therm N --meas M]
+run       : N HMC trajectories of one state (device momenta, graph-driven projection), one JSON line per
+            trajectory in --log (TrajectoryLog): Delta H, the acceptance probability and decision, the
+            average plaquette, the projection's sweep count and the trajectory's wall time.
+
+usage: python studies.py precision [--traj N] [--size L] [--log F] | scale [--traj K] [--size L] | tour [--L 32]
+       | batch [--traj N] | adjoint [--L 48] | distribution [--therm N --meas M]
+       | run [--L 16] [--traj N] [--precision mixed] [--log F]
 """
 import argparse
 import json
@@ -48,6 +53,34 @@ from bench import counted_batch_link_updates  # noqa: E402
 PREC_NAMES = {lqgpu.PRECISION_F64: "f64", lqgpu.PRECISION_MIXED: "mixed", lqgpu.PRECISION_F32: "f32"}
 
 
+class TrajectoryLog:
+    """Per-trajectory diagnostics as JSON lines.  HybridMonteCarloDiagnostic keeps the last
+    trajectory's acceptance probability and decision (prob_replace_last, has_replace_last;
+    src/simulation/monte_carlo/hybrid_monte_carlo.rs:402-410); this log keeps every trajectory's,
+    with Delta H, the average plaquette Re Tr P / 3, the Gauss projection's sweep count and the
+    wall time of the trajectory in milliseconds.  A path of None logs nothing."""
+
+    KEYS = ("trajectory", "form", "beta", "delta_h", "prob", "accepted", "plaquette", "gauss_steps", "ms")
+
+    def __init__(self, path):
+        self.f = open(path, "a") if path else None
+
+    def write(self, **rec):
+        if self.f is None:
+            return
+        missing = [k for k in self.KEYS if k not in rec]
+        if missing:
+            raise ValueError("trajectory record without %s" % ", ".join(missing))
+        rec["accepted"] = bool(rec["accepted"])
+        self.f.write(json.dumps({k: rec[k] for k in self.KEYS}) + "\n")
+        self.f.flush()
+
+    def close(self):
+        if self.f is not None:
+            self.f.close()
+            self.f = None
+
+
 def hbm_peak():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -63,6 +96,7 @@ def study_size(args, L):
 
 
 def precision_study(args):
+    log = TrajectoryLog(args.log)
     dim, L, dt, nmd = 4, args.L, 0.005, 20
     size = study_size(args, L)
     out = {"study": "precision", "dim": dim, "L": L, "size": size, "dt": dt, "md_steps": nmd,
@@ -87,8 +121,9 @@ def precision_study(args):
             u = float(rng.uniform())
             res = {}
             for p, s in states.items():
+                t_start = time.perf_counter()
                 try:
-                    s.hmc_refresh_upload(e_raw)
+                    steps = s.hmc_refresh_upload(e_raw)
                 except lqgpu.LqError as err:
                     # the reference's projection (K = 0.12 relaxation) diverges for large momenta
                     failure = {"trajectory": k, "form": PREC_NAMES[p], "error": str(err)}
@@ -98,6 +133,8 @@ def precision_study(args):
                 s.hmc_decide(a)
                 acc[p] += a
                 res[p] = (h1 - h0, s.average_trace_plaquette().real / 3.0)
+                log.write(trajectory=k, form=PREC_NAMES[p], beta=beta, delta_h=h1 - h0, prob=prob, accepted=a,
+                          plaquette=res[p][1], gauss_steps=steps, ms=1000.0 * (time.perf_counter() - t_start))
                 if (k + 1) % 10 == 0:
                     s.normalize_link_matrices()
             if failure:
@@ -134,6 +171,32 @@ def precision_study(args):
         for s in states.values():
             s.close()
         print(json.dumps({"beta": beta, **out["betas"][str(beta)]}), flush=True)
+    log.close()
+    return out
+
+
+def run_study(args):
+    """N trajectories of one state through the device path, each logged by TrajectoryLog"""
+    prec = {"f64": lqgpu.PRECISION_F64, "mixed": lqgpu.PRECISION_MIXED, "f32": lqgpu.PRECISION_F32}[args.precision]
+    dim, L, beta, dt, nmd = 4, args.L, args.betas[0] if args.betas else 2.0, 0.005, 20
+    log = TrajectoryLog(args.log)
+    uni = np.random.default_rng(7)
+    out = {"study": "run", "dim": dim, "L": L, "beta": beta, "precision": args.precision, "trajectories": args.traj}
+    with lqgpu.State(dim, L, study_size(args, L), beta, prec) as s:
+        s.set_links_random(1)
+        accepted, dh = 0, []
+        for k in range(args.traj):
+            t_start = time.perf_counter()
+            r = s.hmc_trajectory(dt, nmd, 17, k, float(uni.uniform()))
+            plaq = s.average_trace_plaquette().real / 3.0
+            ms = 1000.0 * (time.perf_counter() - t_start)
+            log.write(trajectory=k, form=args.precision, beta=beta, delta_h=r["delta_h"], prob=r["prob"],
+                      accepted=r["accepted"], plaquette=plaq, gauss_steps=r["gauss_steps"], ms=ms)
+            accepted += r["accepted"]
+            dh.append(r["delta_h"])
+        out.update(acceptance=accepted / max(1, args.traj), mean_abs_delta_h=float(np.mean(np.abs(dh))),
+                   plaquette=plaq)
+    log.close()
     return out
 
 
@@ -513,7 +576,9 @@ def tour_study(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "scale", "batch", "adjoint", "distribution", "tour"])
+    ap.add_argument("study", choices=["precision", "scale", "batch", "adjoint", "distribution", "tour", "run"])
+    ap.add_argument("--log", default=None, help="precision, run: per-trajectory JSON lines appended to this file")
+    ap.add_argument("--precision", default="mixed", choices=["f64", "mixed", "f32"], help="run: the state's form")
     ap.add_argument("--traj", type=int, default=None)
     ap.add_argument("--L", type=int, default=32)
     ap.add_argument("--betas", type=float, nargs="*", default=[0.5, 1.0, 2.0, 4.0])
@@ -540,6 +605,12 @@ def main():
         res = distribution_study(args)
     elif args.study == "tour":
         res = tour_study(args)
+    elif args.study == "run":
+        args.traj = args.traj or 20
+        if args.L == 32:
+            args.L = 16
+        args.betas = args.betas if len(args.betas) == 1 else [2.0]
+        res = run_study(args)
     else:
         if args.L == 32:
             args.L = 48

@@ -113,15 +113,87 @@ def _param_counts(src, pattern):
     return counts
 
 
+RUST = os.path.join(REPO, "rust")
+
+
 def test_bindings_declare_every_function_with_its_arity(lqgpu_mod):
-    """the ctypes table and the -sys block of INTEGRATION.md bind every function of the header with as
-    many parameters"""
+    """the ctypes table and the Rust -sys crate (rust/lattice-qcd-gb300-sys/src/lib.rs) bind every function
+    of the header with as many parameters"""
     src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
     c = _param_counts(src, r"\b(lq_[a-z0-9_]+)\s*\(([^)]*)\)\s*;")
-    doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
-    block = doc[doc.index('extern "C" {'):]
+    sys_src = open(os.path.join(RUST, "lattice-qcd-gb300-sys", "src", "lib.rs")).read()
+    block = sys_src[sys_src.index('extern "C" {'):]
     block = block[:block.index("\n}\n")]
     rust = _param_counts(block, r"pub fn (lq_[a-z0-9_]+)\(([^)]*)\)")
     assert sorted(c) == sorted(rust), set(c) ^ set(rust)
     assert {k: c[k] for k in c} == {k: rust[k] for k in c}
     assert {k: c[k] for k in c} == {k: len(lqgpu_mod.SIGNATURES[k][1]) for k in c}
+
+
+def test_checkpoint_load_validates_the_image_on_the_host(lqgpu_mod):
+    """lq_state_load rejects a foreign or truncated image before any device call."""
+    import struct
+
+    G = lqgpu_mod
+    lib = G.load()
+    h = ctypes.c_void_p()
+    assert lib.lq_state_load(None, 0, ctypes.byref(h)) == G.LQ_ERR_INVALID_ARGUMENT
+    assert lib.lq_state_load(b"LQGPUCK1", 8, ctypes.byref(h)) == G.LQ_ERR_INCOMPATIBLE_SIZE
+    bad = b"NOTACKPT" + bytes(104)
+    assert lib.lq_state_load(bad, len(bad), ctypes.byref(h)) == G.LQ_ERR_INVALID_ARGUMENT
+    # a valid header whose declared field sizes the buffer does not hold
+    hdr = b"LQGPUCK1" + struct.pack("<I3i2dq4i2Q4Q", 1, 4, 4, 0, 1000.0, 1.0, 0, 0, 0, 1, 0, 4096, 2048, 0, 0, 0, 0)
+    assert len(hdr) == 112
+    assert lib.lq_state_load(hdr, len(hdr), ctypes.byref(h)) == G.LQ_ERR_INCOMPATIBLE_SIZE
+    assert not h.value
+
+
+def test_rust_sys_constants_match_the_header():
+    """every enumerator of include/lqgpu.h is a constant of the -sys crate with the same value"""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    header = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(LQ_[A-Z0-9_]+)\s*=\s*(\d+)", src)}
+    sys_src = open(os.path.join(RUST, "lattice-qcd-gb300-sys", "src", "lib.rs")).read()
+    rust = {m.group(1): int(m.group(2)) for m in re.finditer(r"pub const (LQ_[A-Z0-9_]+): c_int = (\d+);", sys_src)}
+    assert header == rust, set(header.items()) ^ set(rust.items())
+
+
+def test_rust_crate_implements_the_reference_traits():
+    """the safe crate implements, for its device states, the reference traits a drop-in needs
+    (src/simulation/state.rs:52-278, src/integrator/mod.rs:93-208,
+    src/simulation/monte_carlo/mod.rs:65-77), with every required method"""
+    crate = os.path.join(RUST, "lattice-qcd-gb300", "src")
+    text = {f: open(os.path.join(crate, f)).read() for f in os.listdir(crate) if f.endswith(".rs")}
+    every = "\n".join(text.values())
+
+    def impl_block(trait, ty):
+        m = re.search(r"impl<[^>]*>\s+%s<[^{]*?>\s+for\s+%s\b[^{]*\{" % (trait, ty), every, flags=re.S)
+        assert m, (trait, ty)
+        depth, i = 1, m.end()
+        while depth:
+            depth += {"{": 1, "}": -1}.get(every[i], 0)
+            i += 1
+        return every[m.end():i]
+
+    required = {
+        ("LatticeState", "LatticeStateGpu"): ["link_matrix", "set_link_matrix", "lattice", "beta", "hamiltonian_links"],
+        ("LatticeStateNew", "LatticeStateGpu"): ["new"],
+        ("LatticeState", "LatticeStateGpuEField"): ["link_matrix", "set_link_matrix", "lattice", "beta",
+                                                      "hamiltonian_links"],
+        ("LatticeStateWithEField", "LatticeStateGpuEField"): ["e_field", "set_e_field", "t", "derivative_u",
+                                                                "derivative_e", "hamiltonian_efield"],
+        ("LatticeStateWithEFieldNew", "LatticeStateGpuEField"): ["new"],
+        ("SymplecticIntegrator", "SymplecticEulerGpu"): ["integrate_sync_sync", "integrate_leap_leap",
+                                                         "integrate_sync_leap", "integrate_leap_sync",
+                                                         "integrate_symplectic"],
+        ("MonteCarlo", "HybridMonteCarloGpu"): ["next_element"],
+    }
+    for (trait, ty), methods in required.items():
+        body = impl_block(trait, ty)
+        for m in methods:
+            assert re.search(r"\bfn %s\b" % m, body), (trait, ty, m)
+    assert re.search(r"impl<const D: usize> Clone for LatticeStateGpu<D>", every)
+    assert "lq_state_clone" in text["state.rs"]
+    assert re.search(r"impl<[^>]*>\s+SimulationStateSynchronous<D>\s+for\s+LatticeStateGpuEField<D>", every)
+    # every mode of lq_integrate that the trait's five methods need
+    for mode in ("LQ_SYNC_SYNC", "LQ_LEAP_LEAP", "LQ_SYNC_LEAP", "LQ_LEAP_SYNC", "LQ_SYMPLECTIC"):
+        assert "sys::%s" % mode in text["integrator.rs"], mode

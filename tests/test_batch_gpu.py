@@ -78,7 +78,8 @@ def test_results_do_not_depend_on_tuned_launch_shapes(lqgpu_mod):
                 assert all(v["ms"] > 0.0 for v in t.values())
             b.hmc_run(DT, NSTEPS, 2, MAXG)
             runs.append((b.hmc_results(), [b.link_matrix(e) for e in range(b.n)]))
-    assert np.array_equal(runs[0][0]["delta_h"], runs[1][0]["delta_h"])
+    for key in ("delta_h", "accepted", "gauss_steps", "uniform", "prob"):
+        assert np.array_equal(runs[0][0][key], runs[1][0][key]), key
     for x, y in zip(runs[0][1], runs[1][1]):
         assert np.array_equal(x, y)
 
@@ -169,3 +170,21 @@ def test_tiny_and_ragged_ensembles(lqgpu_mod, precision):
                     assert np.abs(s.link_matrix() - links[e]).max() <= 1e-12
                 else:
                     assert np.array_equal(s.link_matrix(), links[e])
+
+
+def test_eager_kernel_profile_counts_every_launch(lqgpu_mod):
+    """the kernel-time profile of eager trajectories sees every launch, none inside a graph"""
+    G = lqgpu_mod
+    with make_batch(G, G.PRECISION_MIXED) as b:
+        b.profile_enable(True)
+        b.hmc_run(DT, NSTEPS, 1, MAXG, graph=True)
+        assert b.profile_read(reset=True) == (0, 0.0)
+        b.hmc_run(DT, NSTEPS, 2, MAXG, graph=False)
+        n, ms = b.profile_read(reset=True)
+        steps = b.hmc_results()["gauss_steps"].max(axis=1)
+        # per trajectory: draw, Gauss law, the sweeps and their checks (one per 1 or 4 sweeps),
+        # the compensated zeroing, NSTEPS + 1 MD launches, two difference kernels, the accept
+        expected = sum(2 + int(k) + 1 + (int(k) - 1) // 4 + 1 + NSTEPS + 1 + 3 for k in steps)
+        assert n == expected, (n, expected)
+        assert ms > 0.0
+        b.profile_enable(False)

@@ -26,7 +26,8 @@ adjoint   : d<plaq>/dbeta through a 50-step leap-frog at 48^4 by the checkpointe
 distribution: HMC and checkerboard Metropolis on the same lattice and beta give the same average
             plaquette within statistical errors (both sample the Wilson measure).
 
-tour      : every kernel once at 32^4 (for a per-kernel ncu launch list with DRAM bytes).
+tour      : every kernel once at --L (for an ncu launch list: gpu__time_duration.sum alone at full size;
+            captures with more counters on one kernel of a small lattice, --L 12 .. 20).
 
 run       : N HMC trajectories of one state (device momenta, graph-driven projection), one JSON line per
             trajectory in --log (TrajectoryLog): Delta H, the acceptance probability and decision, the

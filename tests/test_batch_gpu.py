@@ -188,3 +188,24 @@ def test_eager_kernel_profile_counts_every_launch(lqgpu_mod):
         assert n == expected, (n, expected)
         assert ms > 0.0
         b.profile_enable(False)
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_lone_state_at_L32_equals_batched_ensemble(lqgpu_mod, dim):
+    """the headline's side length: a lone mixed state and the same lattice as a one-ensemble batch
+    (the batch's persistent kernels over a chunk table) give the same accept decisions, projection
+    steps and links, bitwise"""
+    G = lqgpu_mod
+    with G.Batch(dim, [32], [1000.0], [2.0], G.PRECISION_MIXED) as b:
+        b.set_links_random(LINK_SEED)
+        b.set_seed(SEED, 0)
+        b.hmc_run(DT, 3, 2, MAXG)
+        rb = b.hmc_results()
+        links_b = b.link_matrix(0)
+    with G.State(dim, 32, 1000.0, 2.0, G.PRECISION_MIXED) as s:
+        s.set_links_random(LINK_SEED)
+        for k in range(2):
+            r = s.hmc_trajectory(DT, 3, SEED, k, float(rb["uniform"][k, 0]))
+            assert r["accepted"] == bool(rb["accepted"][k, 0])
+            assert r["gauss_steps"] == rb["gauss_steps"][k, 0]
+        assert np.array_equal(s.link_matrix(), links_b)

@@ -210,22 +210,24 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU arm
-# DRAM bytes (read + write) per link of one k_md kick+drift launch, from one ncu capture of the
-# mixed kernel at 28^4 (994.9 MB for 2,458,624 links); traffic scales with the links of a launch,
-# so the full-size value is this times the links.
-NCU_MD_TRAFFIC_PER_LINK = {"mixed": 994.9e6 / 2458624}
+# DRAM bytes (read + write) per link of one kick+drift launch of the MD kernel (k_md_site), from one
+# ncu capture of the mixed kernel at 28^4 (1045.2 MB for 2,458,624 links); traffic scales with the
+# links of a launch, so the full-size value is this times the links.
+NCU_MD_TRAFFIC_PER_LINK = {"mixed": 1045.2e6 / 2458624}
+MD_KERNEL = "k_md_site (fused force + kick + drift, one thread per site)"
 
 
 # FP64 operations per unit of the FP64 form's kernels (D = 4): FLOP with a multiply-add as 2; the dfma,
 # dmul, dadd instruction counts per unit in parentheses are ncu's at 12^4.
-#   k_md kick+drift per link: 12 staple products, Im Tr(T^a U Sigma), two kicks, E U, the drift
-#     (1372 dfma, 157 dmul, 8 dadd); the final kick-only launch lacks E U and the drift (1272, 131, 8)
+#   k_md_site kick+drift per link: a quarter of a site's 6 plaquettes (shared between the two links of
+#     each) and 12 backward staples, Im Tr(T^a U Sigma), two kicks, E U, the drift (1194 dfma, 174 dmul,
+#     24 dadd); the final kick-only launch lacks E U and the drift (1102, 148, 24)
 #   k_gauss_step per link: u G u^dag and 2 Re Tr(T^a (u G u^dag) G(x+mu)) as Hermitian products, the
 #     update (175, 44, 24)
 #   k_gauss per site: D times U^dag E U as a Hermitian product, the accumulation of G and the residual
 #     (525, 146, 76.5)
 # The compiler contracts some products and sums into multiply-adds.
-FP64_FLOPS = {"md_kick_drift": 2 * 1372 + 157 + 8, "md_kick": 2 * 1272 + 131 + 8,
+FP64_FLOPS = {"md_kick_drift": 2 * 1194 + 174 + 24, "md_kick": 2 * 1102 + 148 + 24,
               "gauss_step": 2 * 175 + 44 + 24, "gauss": 2 * 525 + 146 + 76.5}
 
 
@@ -239,7 +241,7 @@ def fp64_roofline(prof64, n_links, n_sites, md_steps, trajectories, peak):
     out = {"peak_tflops": peak / 1e12, "peak_kind": "measured: lq_fma_peak, FP64 multiply-add chains on every SM",
            "flop_counts": "ncu FP64 instruction counts at 12^4 (2 FLOP per dfma), per link or site: " +
                           json.dumps(FP64_FLOPS)}
-    for name, flops, ms, n in (("k_md", md_flops, md_ms, md_n),
+    for name, flops, ms, n in (("k_md_site", md_flops, md_ms, md_n),
                                ("k_gauss_step", st_n * n_links * FP64_FLOPS["gauss_step"], st_ms, st_n),
                                ("k_gauss", ga_n * n_sites * FP64_FLOPS["gauss"], ga_ms, ga_n)):
         if ms > 0 and n > 0:
@@ -359,7 +361,11 @@ def batch_graph_gap(b, stream, dt, nmd, n_traj, counter):
     import numpy as np
     import torch
 
+    # both runs start from the same links as written back from their FP64 image (a compensated pair read
+    # out and written back is re-split, which need not reproduce the pair the trajectories left behind)
     links = [b.link_matrix(e) for e in range(b.n)]
+    for e, x in enumerate(links):
+        b.set_link_matrix(e, x)
     b.set_seed(3, counter)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -606,7 +612,7 @@ def run_ours(args):
                        "precision": args.precision, "parallelism": "replicas" if world > 1 else "single GPU",
                        "projection_loop": args.projection,
                        "l2": "inputs larger than L2 (links %.0f MB)" % (n_links * 18 * real_bytes / 1e6)},
-            "roofline": {"bound": "hbm", "kernel": "k_md (fused force + kick + drift)", "achieved": achieved,
+            "roofline": {"bound": "hbm", "kernel": MD_KERNEL, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": (NCU_MD_TRAFFIC_PER_LINK[args.precision] * n_links
                                      if args.precision in NCU_MD_TRAFFIC_PER_LINK else None),

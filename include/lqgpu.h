@@ -133,7 +133,9 @@ int lq_state_info(const lq_state *s, int *dim, int *L, double *size, double *bet
 int lq_state_set_beta(lq_state *s, double beta);
 /* choose the link update of the HMC proposal (lq_link_update); Euler, the reference's, by default */
 int lq_state_set_link_update(lq_state *s, int link_update);
-/* Device bytes held by the state (links buffers, E, Gauss buffer, staging). */
+/* Device bytes held by the state (links buffers, E, Gauss buffer, staging; an FP64 state adds a
+ * scratch array of 82 reals per link: its Gauss projection's transport tables and its MD step's
+ * force parts). */
 int lq_state_device_bytes(const lq_state *s, size_t *bytes);
 
 /* ---------------------------------------------------------------- fields */

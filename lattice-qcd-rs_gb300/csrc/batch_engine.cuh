@@ -202,6 +202,26 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md_batch(BView<T> v, 
     }
 }
 
+// the same step with one thread per site (md_site), as the single-lattice kernel of this precision runs it
+template <int D, typename T, bool COMP, int MODE>
+__global__ void __launch_bounds__(kMdSiteBlock, MinBlocks<T>::md_site)
+    k_md_site_batch(BView<T> v, int rin, int rout, int ein, int eout, int k1_on) {
+    static_assert(kChunk == kMdSiteBlock, "one chunk per block");
+    __shared__ T fs[(D - 1) * 8][kMdSiteBlock];
+    for (uint32_t w = blockIdx.x; w < v.n_chunks; w += gridDim.x) {
+        const uint2 c = v.chunks[w];
+        const BatchEns &en = v.ens[c.x];
+        const uint32_t site = c.y + threadIdx.x;
+        if (site >= en.V) continue;
+        const int cur = v.run[c.x].cur;
+        const size_t ub = (size_t)en.tile0 * (D * 9 * kTile), eb = (size_t)en.tile0 * (D * 8 * kTile);
+        const T kh = coef<T>(en.kh_f, en.kh_d);
+        md_site<D, T, COMP, MODE>(sel_u(v, (cur + rin) % 3) + ub, sel_u(v, (cur + rout) % 3) + ub, sel_e(v, ein) + eb,
+                                  sel_e(v, eout) + eb, geo_of<D>(en), site, k1_on ? kh : T(0), kh,
+                                  coef<T>(en.dr_f, en.dr_d), v.ulo, v.elo, fs, threadIdx.x);
+    }
+}
+
 // partial row 0 <- per-chunk sum Re Tr[P(U[r_new]) - P(U[r_old])]
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128) k_plaquette_delta_batch(BView<T> v, int r_old, int r_new) {
@@ -437,13 +457,19 @@ template <int D, typename T, bool COMP> struct BatchEngine {
                                                       b.flag, h, use_handle);
         return cudaGetLastError();
     }
-    static cudaError_t md(Batch &b, int rin, int rout, int ein, int eout, int mode, int k1_on) {
-        const uint32_t n = b.n_chunks * D;
-        const uint32_t gsz = grid(b, BK_MD, n);
-        const int order = b.shape[BK_MD].order;
+    template <int M> static void launch_md(Batch &b, int rin, int rout, int ein, int eout, int k1_on) {
         const BView<T> v = view(b);
+        if constexpr (MdSite<T>::on && (M & MD_KICK)) {
+            k_md_site_batch<D, T, COMP, M>
+                <<<grid(b, BK_MD, b.n_chunks), kChunk, 0, b.stream>>>(v, rin, rout, ein, eout, k1_on);
+        } else {
+            k_md_batch<D, T, COMP, M><<<grid(b, BK_MD, b.n_chunks * D), kChunk, 0, b.stream>>>(
+                v, rin, rout, ein, eout, k1_on, b.shape[BK_MD].order);
+        }
+    }
+    static cudaError_t md(Batch &b, int rin, int rout, int ein, int eout, int mode, int k1_on) {
 #define LQ_MDB_CASE(M)                                                                                                 \
-    case (M): k_md_batch<D, T, COMP, (M)><<<gsz, kChunk, 0, b.stream>>>(v, rin, rout, ein, eout, k1_on, order); break;
+    case (M): launch_md<(M)>(b, rin, rout, ein, eout, k1_on); break;
         switch (mode) {
             LQ_MDB_CASE(MD_KICK)
             LQ_MDB_CASE(MD_KICK | MD_DRIFT)
@@ -492,7 +518,12 @@ template <int D, typename T, bool COMP> struct BatchEngine {
         cudaError_t err = cudaSuccess;
         switch (cls) {
         case BK_MD:
-            err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_md_batch<D, T, COMP, MD_KICK | MD_DRIFT>, kChunk, 0);
+            if constexpr (MdSite<T>::on)
+                err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_md_site_batch<D, T, COMP, MD_KICK | MD_DRIFT>,
+                                                                    kChunk, 0);
+            else
+                err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_md_batch<D, T, COMP, MD_KICK | MD_DRIFT>,
+                                                                    kChunk, 0);
             break;
         case BK_SWEEP: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_batch<D, T>, kChunk, 0); break;
         case BK_GAUSS: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gauss_batch<D, T>, kChunk, 0); break;

@@ -2,6 +2,8 @@
 #pragma once
 #include <math.h>
 
+#include <type_traits>
+
 #include "adjoint.cuh"
 #include "kernels.cuh"
 #include "state.hpp"
@@ -59,11 +61,25 @@ template <int D, typename T, bool COMP> struct Engine {
     // 32 sites x D directions per block measured 13% slower at 32^4)
     static dim3 md_grid_k(const State &s) { return dim3(((s.V + 127) / 128) * D, 1, 1); }
     static unsigned md_block_k() { return 128; }
+    // The FP64 state: k_md_plaq + k_md_update.  Otherwise one thread per site (k_md_site) or per link
+    // (k_md), as MdSite<T> selects; a drift alone has no force to share and runs per link.
+    template <int M>
+    static void launch_md(State &s, const void *Uin, void *Uout, const void *Ein, void *Eout, T k1, T k2, T drift) {
+        if constexpr (LQ_MD_SPLIT_FP64 && std::is_same<T, double>::value && (M & MD_KICK)) {
+            k_md_plaq<D, T><<<(s.V + 127) / 128, 128, 0, s.stream>>>((const V2<T> *)Uin, (T *)s.R, geo(s));
+            k_md_update<D, T, COMP, M><<<md_grid_k(s), md_block_k(), 0, s.stream>>>(
+                (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, (const T *)s.R, geo(s), k1, k2, drift);
+        } else if constexpr (MdSite<T>::on && (M & MD_KICK)) {
+            k_md_site<D, T, COMP, M><<<(s.V + kMdSiteBlock - 1) / kMdSiteBlock, kMdSiteBlock, 0, s.stream>>>(
+                (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, geo(s), k1, k2, drift);
+        } else {
+            k_md<D, T, COMP, M><<<md_grid_k(s), md_block_k(), 0, s.stream>>>(
+                (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, geo(s), k1, k2, drift);
+        }
+    }
     static cudaError_t force(State &s, const void *U, void *out, double scale) {
-        const dim3 grid = md_grid_k(s);
         // kick only: the output links are never written (null)
-        k_md<D, T, COMP, MD_KICK><<<grid, md_block_k(), 0, s.stream>>>((const V2<T> *)U, (V2<T> *)nullptr, (const T *)out,
-                                                                       (T *)out, geo(s), T(0), (T)scale, T(0));
+        launch_md<MD_KICK>(s, U, nullptr, out, out, T(0), (T)scale, T(0));
         return cudaGetLastError();
     }
     static cudaError_t link_rotate(State &s, void *U, uint32_t site, int mu, int a, double angle) {
@@ -83,15 +99,8 @@ template <int D, typename T, bool COMP> struct Engine {
         // drift coefficient dt * sqrt(2 C_A) / size
         const double cu = sqrt(2.0 * 3.0) / s.size * dt;
         const T k1 = (T)(h1 * ce), k2 = (T)(h2 * ce), drift = (T)cu;
-        const Geo<D> g = geo(s);
-        const dim3 grid = md_grid_k(s);
-        const unsigned block = md_block_k();
-        const V2<T> *in = (const V2<T> *)Uin;
-        V2<T> *out = (V2<T> *)Uout;
-        const T *ei = (const T *)Ein;
-        T *eo = (T *)Eout;
 #define LQ_MD_CASE(M)                                                                                                  \
-    case (M): k_md<D, T, COMP, (M)><<<grid, block, 0, s.stream>>>(in, out, ei, eo, g, k1, k2, drift); break;
+    case (M): launch_md<(M)>(s, Uin, Uout, Ein, Eout, k1, k2, drift); break;
         switch (mode) {
             LQ_MD_CASE(MD_KICK)
             LQ_MD_CASE(MD_DRIFT)
@@ -128,6 +137,35 @@ template <int D, typename T, bool COMP> struct Engine {
         const dim3 grid(((s.V + 127) / 128) * D, 1, 1);
         k_gauss_step<D, T, COMP><<<grid, 128, 0, s.stream>>>((const V2<T> *)U, (T *)s.E, (const T *)s.G, geo(s));
         return cudaGetLastError();
+    }
+    static constexpr bool kAdjointProjection = std::is_same<T, double>::value;
+    static cudaError_t adjoint_links(State &s, const void *U) {
+        if constexpr (kAdjointProjection) {
+            k_adjoint_links<D, T><<<((s.V + 127) / 128) * D, 128, 0, s.stream>>>((const V2<T> *)U, (T *)s.R, geo(s));
+            return cudaGetLastError();
+        } else {
+            return cudaErrorNotSupported;
+        }
+    }
+    static cudaError_t gauss_adj(State &s, uint32_t *n_partials) {
+        if constexpr (kAdjointProjection) {
+            const uint32_t blocks = (s.V + 255) / 256;
+            k_gauss_adj<D, T><<<blocks, 256, 0, s.stream>>>((const T *)s.R, (const T *)s.E, (T *)s.G, geo(s),
+                                                            s.partial);
+            *n_partials = blocks;
+            return cudaGetLastError();
+        } else {
+            return cudaErrorNotSupported;
+        }
+    }
+    static cudaError_t gauss_step_adj(State &s) {
+        if constexpr (kAdjointProjection) {
+            k_gauss_step_adj<D, T><<<((s.V + 127) / 128) * D, 128, 0, s.stream>>>((const T *)s.R, (T *)s.E,
+                                                                                    (const T *)s.G, geo(s));
+            return cudaGetLastError();
+        } else {
+            return cudaErrorNotSupported;
+        }
     }
     static cudaError_t gauss_to_aos(State &s, double *d_out) {
         k_gauss_to_aos<T><<<(s.V + 255) / 256, 256, 0, s.stream>>>((const T *)s.G, d_out, s.V);
@@ -241,7 +279,11 @@ template <int D, typename T, bool COMP> struct Engine {
     static const Ops *table() {
         static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
                                 efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
-                                gauss_step,     gauss_to_aos,   plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
+                                gauss_step,     gauss_to_aos,
+                                kAdjointProjection ? adjoint_links : nullptr,
+                                kAdjointProjection ? gauss_adj : nullptr,
+                                kAdjointProjection ? gauss_step_adj : nullptr,
+                                plaquette,     plaquette_delta, efield_sumsq, efield_sumsq_delta,
                                 normalize,      finalize,       force,         link_rotate,
                                 adj_init,       adj_kick,       adj_drift,     dot,
                                 cot_links_to_aos, cot_efield_to_aos, clover_fields, mc_sweep, efield_hi_from_aos};

@@ -86,7 +86,31 @@ template <typename T> using V2 = typename vec2_t<T>::type;
 #define LQ_SWEEP_MIN_BLOCKS 4
 #endif
 
+// The MD step runs one thread per site (k_md_site, the plaquettes shared between a site's links) or
+// one thread per link (k_md); LQ_MD_SITE_FP64 / LQ_MD_SITE_FP32 choose per precision.  The FP64
+// state runs it as two launches (k_md_plaq + k_md_update, every plaquette formed once) unless
+// LQ_MD_SPLIT_FP64 is 0.
+#ifndef LQ_MD_SPLIT_FP64
+#define LQ_MD_SPLIT_FP64 1
+#endif
+#ifndef LQ_MD_SITE_FP64
+#define LQ_MD_SITE_FP64 1
+#endif
+#ifndef LQ_MD_SITE_FP32
+#define LQ_MD_SITE_FP32 1
+#endif
+#ifndef LQ_MD_SITE_MIN_BLOCKS
+#define LQ_MD_SITE_MIN_BLOCKS 4
+#endif
+#ifndef LQ_MD_SITE_MIN_BLOCKS_FP64
+#define LQ_MD_SITE_MIN_BLOCKS_FP64 1
+#endif
+constexpr int kMdSiteBlock = 128;
+template <typename T> struct MdSite {
+    static constexpr bool on = sizeof(T) == 8 ? LQ_MD_SITE_FP64 : LQ_MD_SITE_FP32;
+};
 template <typename T> struct MinBlocks {
+    static constexpr int md_site = sizeof(T) == 4 ? LQ_MD_SITE_MIN_BLOCKS : LQ_MD_SITE_MIN_BLOCKS_FP64;
     static constexpr int md = sizeof(T) == 4 ? LQ_MD_MIN_BLOCKS : 1;
     static constexpr int sweep = sizeof(T) == 4 ? LQ_SWEEP_MIN_BLOCKS : 1;
 };
@@ -244,13 +268,29 @@ enum : int { MD_KICK = 1, MD_DRIFT = 2, MD_DRIFT_OLD_E = 4, MD_EXP = 8, MD_REUNI
 //         orthonormalize_matrix to the result (in double, from hi + lo).
 // md_update applies the kick (with the staple sum sig) and the drift to link (site, mu), reading
 // the link and its momenta from Uin / Ein (lo halves at ulo / elo elements further).
+// md_kick_drift: md_update's kick and drift of link (site, mu) from its force coefficients
+// f^a = Im Tr(T^a U_mu(x) Sigma_mu(x)) and the link u = U_mu(x) itself.
+template <int D, typename T, bool COMP, int MODE>
+__device__ __forceinline__ void md_kick_drift(const T (&f)[8], mat3<T> &u, const V2<T> *__restrict__ Uin, const T *Ein,
+                                              V2<T> *__restrict__ Uout, T *Eout, bool copy_e, uint32_t site, int mu,
+                                              T k1, T k2, T drift, size_t ulo, size_t elo);
+
 template <int D, typename T, bool COMP, int MODE>
 __device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *__restrict__ Uin, const T *Ein,
                                           V2<T> *__restrict__ Uout, T *Eout, bool copy_e, uint32_t site, int mu,
                                           T k1, T k2, T drift, size_t ulo, size_t elo) {
-    const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
     mat3<T> u;
-    load_link<T>(Uin, ui, u);
+    load_link<T>(Uin, tix(site, D * 9, mu * 9), u);
+    T f[8];
+    if (MODE & MD_KICK) im_tr_generators_of_product(u, sig, f);
+    md_kick_drift<D, T, COMP, MODE>(f, u, Uin, Ein, Uout, Eout, copy_e, site, mu, k1, k2, drift, ulo, elo);
+}
+
+template <int D, typename T, bool COMP, int MODE>
+__device__ __forceinline__ void md_kick_drift(const T (&f)[8], mat3<T> &u, const V2<T> *__restrict__ Uin, const T *Ein,
+                                              V2<T> *__restrict__ Uout, T *Eout, bool copy_e, uint32_t site, int mu,
+                                              T k1, T k2, T drift, size_t ulo, size_t elo) {
+    const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
     T e[8], el[8], e_old[8];
     load_efield<T>(Ein, ei, e);
     if (COMP) load_efield<T>(Ein + elo, ei, el);
@@ -260,8 +300,6 @@ __device__ __forceinline__ void md_update(const mat3<T> &sig, const V2<T> *__res
         e_old[a] = e[a];
     }
     if (MODE & MD_KICK) {
-        T f[8];
-        im_tr_generators_of_product(u, sig, f);
         if (COMP) {
             // compensated storage: one exact-sum update with both half-kicks (the separate
             // adds of the FP64 form only reproduce the reference's FP64 rounding)
@@ -354,6 +392,89 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
     const size_t ulo = nt * D * 9 * kTile, elo = nt * D * 8 * kTile;
     if (site >= g.V) return;
     md_link<D, T, COMP, MODE>(Uin, Uout, Ein, Eout, g, site, mu, k1, k2, drift, ulo, elo);
+}
+
+// k_md_site: the MD step with one thread per site and its D links, the plaquette products shared
+// between the links that need them.  For the links (x, mu) and (x, nu) of one site, the +nu staple of
+// the first and the +mu staple of the second close the same plaquette P_mu,nu(x) =
+// U_mu(x) U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag: U_mu(x) S+_mu,nu(x) = P and U_nu(x) S+_nu,mu(x) =
+// P^dag, so Im Tr(T^a .) of one product serves both links with opposite signs.  Per site the forward
+// staples then cost D(D-1)/2 plaquettes (two products and one projected product each) instead of
+// D(D-1) staples of two products and their share of U Sigma: 4788 multiply-add-sized steps per site
+// at D = 4 instead of 5544.  The backward staples keep staple_sum's products.  Each link's force
+// is complete once the planes (mu, nu > mu) and (nu < mu, mu) and its backward staples are summed,
+// and that link is kicked and drifted by md_update's arithmetic before the next direction.  The
+// force is summed per plaquette rather than as one staple matrix, so the results differ from k_md's
+// by rounding (the FP64 form's parity with the reference is unchanged at 1e-12).
+template <int D, typename T, bool COMP, int MODE>
+__device__ __forceinline__ void md_site(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout,
+                                        const Geo<D> &g, uint32_t site, T k1, T k2, T drift, size_t ulo, size_t elo,
+                                        T (&fs)[(D - 1) * 8][kMdSiteBlock], unsigned t) {
+    static_assert(MODE & MD_KICK, "the site kernel computes the force");
+    uint32_t c[D];
+    site_coords(g, site, c);
+#pragma unroll
+    for (int a = 0; a < (D - 1) * 8; ++a) fs[a][t] = T(0);
+    // one direction at a time: with the directions unrolled the compiler spills (kilobytes of local
+    // memory in the FP64 and several FP32 modes)
+#pragma unroll 1
+    for (int mu = 0; mu < D; ++mu) {
+        const uint32_t xpmu = fwd(g, site, c[mu], mu);
+        mat3<T> umu;
+        load_link<T>(Uin, tix(site, D * 9, mu * 9), umu);
+        T f[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) f[a] = mu == 0 ? T(0) : fs[(mu - 1) * 8 + a][t];
+        // forward plaquettes of the planes (mu, nu > mu): P = U_mu(x) U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag
+#pragma unroll
+        for (int nu = mu + 1; nu < D; ++nu) {
+            mat3<T> p, q, A;
+            load_link<T>(Uin, tix(xpmu, D * 9, nu * 9), q);
+            mul_nn(umu, q, A);
+            load_link<T>(Uin, tix(fwd(g, site, c[nu], nu), D * 9, mu * 9), q);
+            mul_na(A, q, p);
+            load_link<T>(Uin, tix(site, D * 9, nu * 9), q);
+            T pf[8];
+            im_tr_generators_of_product_na(p, q, pf);
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                f[a] += pf[a];
+                fs[(nu - 1) * 8 + a][t] -= pf[a];
+            }
+        }
+        // backward staples of (x, mu): U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)
+        mat3<T> sig;
+        mat_zero(sig);
+#pragma unroll
+        for (int nu = 0; nu < D; ++nu) {
+            if (nu == mu) continue;
+            mat3<T> a, b, w;
+            const uint32_t xmnu = bwd(g, site, c[nu], nu);
+            load_link<T>(Uin, tix(xmnu, D * 9, mu * 9), a);
+            load_link<T>(Uin, tix(bwd(g, xpmu, c[nu], nu), D * 9, nu * 9), b);
+            mul_nn(a, b, w);
+            load_link<T>(Uin, tix(xmnu, D * 9, nu * 9), a);
+            mul_an_acc(w, a, sig);
+        }
+        T fb[8];
+        im_tr_generators_of_product(umu, sig, fb);
+#pragma unroll
+        for (int a = 0; a < 8; ++a) f[a] += fb[a];
+        md_kick_drift<D, T, COMP, MODE>(f, umu, Uin, Ein, Uout, Eout, Eout != Ein, site, mu, k1, k2, drift, ulo, elo);
+    }
+}
+
+template <int D, typename T, bool COMP, int MODE>
+__global__ void __launch_bounds__(kMdSiteBlock, MinBlocks<T>::md_site)
+    k_md_site(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout, Geo<D> g, T k1, T k2,
+              T drift) {
+    // the parts of later directions' forces from the planes (mu, nu > mu), one column per thread
+    __shared__ T fs[(D - 1) * 8][kMdSiteBlock];
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    if (site >= g.V) return;
+    const size_t nt = tiles_of(g.V);
+    md_site<D, T, COMP, MODE>(Uin, Uout, Ein, Eout, g, site, k1, k2, drift, nt * D * 9 * kTile, nt * D * 8 * kTile, fs,
+                              threadIdx.x);
 }
 
 // U <- exp(i angle T^a) U for one link (finite-difference probes of the action)
@@ -514,6 +635,317 @@ __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U,
     projection_step<T, COMP>(u, gx, gxc, gp, e, el);
     store_efield<T>(E, ei, e);
     if (COMP) store_efield<T>(E + elo, ei, el);
+}
+
+// ---- the FP64 projection in the adjoint representation ----
+// The projection changes E only: its links are fixed.  So the maps X -> U X U^dag and
+// X -> U^dag X U of every link on Hermitian 3x3 matrices are formed once per projection
+// (k_adjoint_links), and every parallel transport in the sweeps becomes a real 9x9
+// matrix-vector product instead of two complex 3x3 products.  A Hermitian X is held as its 9
+// components x^a = 2 Re Tr(T^a X) (a < 8) and x^8 = Tr X, X = sum x^a T^a + (x^8 / 3) 1.  The
+// trace is carried because the links are not exactly unitary: the leap-frog's first-order link
+// update leaves |U U^dag - 1| ~ 1e-8 after a trajectory, and the reference transports with the
+// full matrices, so U^dag E U has a trace and G(x) with it.  The two maps share one table per link:
+//   R_ab = 2 Re Tr(T^a U T^b U^dag)      (U X U^dag: R;  U^dag X U: R^T, on the generator block)
+//   A_a = 2 Re Tr(T^a U U^dag),  B_a = 2 Re Tr(T^a U^dag U),  t = Tr(U U^dag)
+//   U X U^dag:  y^a = R_ab x^b + A_a x^8 / 3,   y^8 = B_b x^b / 2 + t x^8 / 3
+//   U^dag X U:  y^a = R_ba x^b + B_a x^8 / 3,   y^8 = A_b x^b / 2 + t x^8 / 3
+// The arithmetic is k_gauss / k_gauss_step's up to rounding: the FP64 state's projection, bound
+// by its FP64 multiply-add rate.
+//
+// Layout of the table: the kAdjReals reals of the link (site, mu) fill planes mu*kAdjReals ..
+// of a tile (tix(site, D * kAdjReals, mu * kAdjReals)): R row-major, A, B, t and one pad, packed in
+// double2 pairs like the momenta (a thread moves a row of R with four 128-bit accesses).  G(x):
+// kGaussReals planes per site (the 9 components and one pad), tix(site, kGaussReals, 0), packed the
+// same way.
+constexpr int kAdjReals = 82;
+constexpr int kAdjA = 64, kAdjB = 72, kAdjT = 80;
+constexpr int kGaussReals = 10;
+template <int N>
+__device__ __forceinline__ void load_packed(const double *__restrict__ A, size_t idx, int first, double *v) {
+    const size_t lane = idx & 31;
+    const double2 *q = reinterpret_cast<const double2 *>(A + (idx - lane)) + lane;
+#pragma unroll
+    for (int j = 0; j < N / 2; ++j) {
+        const double2 x = q[(first / 2 + j) * kTile];
+        v[2 * j] = x.x;
+        v[2 * j + 1] = x.y;
+    }
+}
+template <int N>
+__device__ __forceinline__ void store_packed(double *__restrict__ A, size_t idx, int first, const double *v) {
+    const size_t lane = idx & 31;
+    double2 *q = reinterpret_cast<double2 *>(A + (idx - lane)) + lane;
+#pragma unroll
+    for (int j = 0; j < N / 2; ++j) q[(first / 2 + j) * kTile] = make_double2(v[2 * j], v[2 * j + 1]);
+}
+
+// the transport table of every link, one thread per link (directions fastest in the block order, as
+// k_gauss_step).  Row a of R holds the generator components of Q^a = U^dag T^a U, whose entries are
+// sums of P^{rc}_ij = conj(U_ri) U_cj over the nonzero entries (r, c) of T^a (adjoint_to_matrix's
+// Gell-Mann basis): with S = P^{rc} + P^{cr} and A = P^{cr} - P^{rc},
+//   (r, c) = (0, 1): Q^0 = S / 2, Q^1 = i A / 2;  (0, 2): Q^3, Q^4;  (1, 2): Q^5, Q^6 likewise;
+//   Q^2 = (P^{00} - P^{11}) / 2,  Q^7 = (P^{00} + P^{11} - 2 P^{22}) / (2 sqrt(3)).
+// Column b of R is 2 Re Tr(T^b Q^a): 2 Re Q_01, -2 Im Q_01, Q_00 - Q_11, 2 Re Q_02, -2 Im Q_02,
+// 2 Re Q_12, -2 Im Q_12, (Q_00 + Q_11 - 2 Q_22) / sqrt(3) (Q Hermitian).
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_adjoint_links(const V2<T> *__restrict__ U, T *__restrict__ R, Geo<D> g) {
+    static_assert(sizeof(T) == 8, "the adjoint projection is the FP64 state's");
+    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.x % D;
+    if (site >= g.V) return;
+    mat3<T> u;
+    load_link<T>(U, tix(site, D * 9, mu * 9), u);
+    const size_t ri = tix(site, D * kAdjReals, mu * kAdjReals);
+    auto P = [&](int r, int i, int c, int j) { // conj(U_ri) U_cj
+        const cpx<T> x = u.e[r * 3 + i], y = u.e[c * 3 + j];
+        return cmk(fma(x.re, y.re, x.im * y.im), fma(x.re, y.im, -x.im * y.re));
+    };
+    const T r3 = T(2.0 * kOneOver2Sqrt3); // 1/sqrt(3)
+    T Rm[8][8];
+    // off-diagonal entries (i, j) of every Q^a, stored as R columns c0 = 2 Re Q_ij, c0 + 1 = -2 Im Q_ij
+    // (a = P^{rc}, b = P^{cr}: Q^{g} = (a + b) / 2, Q^{g+1} = i (b - a) / 2)
+    auto offdiag = [&](int i, int j, int c0) {
+        const int rc[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        const int gs[3] = {0, 3, 5};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const cpx<T> a = P(rc[k][0], i, rc[k][1], j), b = P(rc[k][1], i, rc[k][0], j);
+            Rm[gs[k]][c0] = a.re + b.re;
+            Rm[gs[k]][c0 + 1] = -(a.im + b.im);
+            Rm[gs[k] + 1][c0] = a.im - b.im;
+            Rm[gs[k] + 1][c0 + 1] = a.re - b.re;
+        }
+        const cpx<T> p00 = P(0, i, 0, j), p11 = P(1, i, 1, j), p22 = P(2, i, 2, j);
+        Rm[2][c0] = p00.re - p11.re;
+        Rm[2][c0 + 1] = p11.im - p00.im;
+        Rm[7][c0] = r3 * fma(T(-2), p22.re, p00.re + p11.re);
+        Rm[7][c0 + 1] = -r3 * fma(T(-2), p22.im, p00.im + p11.im);
+    };
+    offdiag(0, 1, 0);
+    offdiag(0, 2, 3);
+    offdiag(1, 2, 5);
+    // the real diagonal entries Q^a_ii (P^{cr}_ii = conj(P^{rc}_ii)): columns 2 (Q_00 - Q_11) and 7
+    // ((Q_00 + Q_11 - 2 Q_22) / sqrt(3))
+    T d[3][8];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const T p00 = P(0, i, 0, i).re, p11 = P(1, i, 1, i).re, p22 = P(2, i, 2, i).re;
+        const int rc[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        const int gs[3] = {0, 3, 5};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const cpx<T> a = P(rc[k][0], i, rc[k][1], i);
+            d[i][gs[k]] = a.re; // (a + conj(a)) / 2
+            d[i][gs[k] + 1] = a.im; // i (conj(a) - a) / 2
+        }
+        d[i][2] = T(0.5) * (p00 - p11);
+        d[i][7] = T(kOneOver2Sqrt3) * fma(T(-2), p22, p00 + p11);
+    }
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        Rm[a][2] = d[0][a] - d[1][a];
+        Rm[a][7] = r3 * fma(T(-2), d[2][a], d[0][a] + d[1][a]);
+    }
+#pragma unroll
+    for (int a = 0; a < 8; ++a) store_packed<8>(R, ri, a * 8, Rm[a]);
+    mat3<T> w;
+    T v[8];
+    mul_na(u, u, w); // U U^dag
+    two_re_tr_generators(w, v);
+    store_packed<8>(R, ri, kAdjA, v);
+    const T tr[2] = {w.e[0].re + w.e[4].re + w.e[8].re, T(0)};
+    mul_an(u, u, w); // U^dag U
+    two_re_tr_generators(w, v);
+    store_packed<8>(R, ri, kAdjB, v);
+    store_packed<2>(R, ri, kAdjT, tr);
+}
+
+// G(x) (9 components) and the residual partials (k_gauss's Gauss law), E traceless:
+//   G(x) = sum_mu [E_mu(x) - U_mu(x-mu)^dag E_mu(x-mu) U_mu(x-mu)]
+template <int D, typename T>
+__global__ void __launch_bounds__(256) k_gauss_adj(const T *__restrict__ R, const T *__restrict__ E,
+                                                   T *__restrict__ G, Geo<D> g, double *__restrict__ partial) {
+    static_assert(sizeof(T) == 8, "the adjoint projection is the FP64 state's");
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    double res[1] = {0.0};
+    if (site < g.V) {
+        uint32_t c[D];
+        site_coords(g, site, c);
+        T gs[kGaussReals];
+#pragma unroll
+        for (int a = 0; a < kGaussReals; ++a) gs[a] = T(0);
+#pragma unroll
+        for (int mu = 0; mu < D; ++mu) {
+            const uint32_t xm = bwd(g, site, c[mu], mu);
+            T ex[8], em[8], av[8];
+            load_efield<T>(E, tix(site, D * 8, mu * 8), ex);
+            load_efield<T>(E, tix(xm, D * 8, mu * 8), em);
+#pragma unroll
+            for (int a = 0; a < 8; ++a) gs[a] += ex[a];
+            const size_t ri = tix(xm, D * kAdjReals, mu * kAdjReals);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                T row[8];
+                load_packed<8>(R, ri, b * 8, row);
+#pragma unroll
+                for (int a = 0; a < 8; ++a) gs[a] = fma(-row[a], em[b], gs[a]);
+            }
+            load_packed<8>(R, ri, kAdjA, av);
+            T tr = T(0);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) tr = fma(av[b], em[b], tr);
+            gs[8] = fma(T(-0.5), tr, gs[8]);
+        }
+        store_packed<kGaussReals>(G, tix(site, kGaussReals, 0), 0, gs);
+        T sum = T(0);
+#pragma unroll
+        for (int a = 0; a < 8; ++a) sum += gs[a];
+        res[0] = (double)(fabs(sum) * T(0.5));
+    }
+    block_reduce_store<1>(res, partial, blockIdx.x, gridDim.x);
+}
+
+// One projection step on every link from the components of G (k_gauss_step's arithmetic):
+//   e^a += 0.12 (2 Re Tr(T^a H G(x+mu)) - 2 Re Tr(T^a G(x))),  H = U G(x) U^dag
+// with 2 Re Tr(T^a H P) = 2 Re Tr(T^a H0 P0) + h^8 p^a / 3 + p^8 h^a / 3 for H0, P0 the
+// traceless parts; the factor 0.12 rides on the constants of each term.
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_gauss_step_adj(const T *__restrict__ R, T *__restrict__ E,
+                                                        const T *__restrict__ G, Geo<D> g) {
+    static_assert(sizeof(T) == 8, "the adjoint projection is the FP64 state's");
+    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.x % D;
+    if (site >= g.V) return;
+    uint32_t c[D];
+    site_coords(g, site, c);
+    T gx[kGaussReals], gp[kGaussReals], h[8], e[8], v[8];
+    load_packed<kGaussReals>(G, tix(site, kGaussReals, 0), 0, gx);
+    load_packed<kGaussReals>(G, tix(fwd(g, site, c[mu], mu), kGaussReals, 0), 0, gp);
+    const size_t ri = tix(site, D * kAdjReals, mu * kAdjReals);
+    const T g8 = gx[8] * T(1.0 / 3.0);
+    load_packed<8>(R, ri, kAdjA, v);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        T row[8];
+        load_packed<8>(R, ri, a * 8, row);
+        T acc = v[a] * g8;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc = fma(row[b], gx[b], acc);
+        h[a] = acc;
+    }
+    T tr[2];
+    load_packed<8>(R, ri, kAdjB, v);
+    load_packed<2>(R, ri, kAdjT, tr);
+    T h8 = T(0);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) h8 = fma(v[b], gx[b], h8);
+    h8 = fma(T(0.5), h8, tr[0] * g8);
+    const T K = T(0.12);
+    const T kh8 = K * (h8 * T(1.0 / 3.0)), kp8 = K * (gp[8] * T(1.0 / 3.0));
+    const size_t ei = tix(site, D * 8, mu * 8);
+    load_efield<T>(E, ei, e);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) e[a] = fma(kp8, h[a], fma(kh8, gp[a], fma(-K, gx[a], e[a])));
+    two_re_tr_generators_of_traceless_product(h, gp, K, e);
+    store_efield<T>(E, ei, e);
+}
+
+// ---- the FP64 state's MD step in two launches ----
+// k_md_plaq forms each plaquette's products once and hands the force on all four of its links: with
+// a = U_mu(x), b = U_nu(x+mu), c = U_mu(x+nu), d = U_nu(x), A = a b, B = d c (mu < nu),
+//   (x, mu) +Im Tr(T^a A B^dag)   and  (x, nu) -Im Tr(T^a A B^dag)   (the +nu / +mu staples, P = A B^dag)
+//   (x+nu, mu)  Im Tr(T^a c A^dag d)                                   (its -nu staple b^dag a^dag d)
+//   (x+mu, nu)  Im Tr(T^a b B^dag a)                                   (its -mu staple c^dag d^dag a)
+// 4 products and 3 projections per plaquette, against 6 products and 2 projections (each a share of
+// one staple-sum projection) when the backward staples are formed again by the sites that need them.
+// The parts (twice their value: the projections' factor 1/2 is applied once, to the kick factors)
+// land in the scratch array, D slots of 8 reals per link: slot 0 the forward part (the
+// planes through the link's own site, summed in plane order), slot 1 + k the backward part from the
+// k-th direction other than the link's; k_md_update sums the slots in that order and applies
+// md_update's kick and drift.  FP64 only: the FP64 state is bound by its multiply-add rate, where
+// the shared products turn into time, while the FP32 forms are bound by issue and latency and would
+// pay the slots' extra traffic.  Scratch layout: tix(site, D * D * 8, mu * D * 8), packed double2
+// pairs like the momenta.
+template <int D> __device__ __forceinline__ int md_slot(int from, int link_dir) {
+    return 1 + (from < link_dir ? from : from - 1);
+}
+
+template <int D, typename T>
+__global__ void __launch_bounds__(128) k_md_plaq(const V2<T> *__restrict__ U, T *__restrict__ F, Geo<D> g) {
+    static_assert(sizeof(T) == 8, "the split MD step is the FP64 state's");
+    __shared__ T fs[D * 8][128]; // forward parts, one column per thread
+    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    if (site >= g.V) return;
+    const unsigned t = threadIdx.x;
+    uint32_t c[D];
+    site_coords(g, site, c);
+#pragma unroll
+    for (int a = 0; a < D * 8; ++a) fs[a][t] = T(0);
+#pragma unroll 1
+    for (int mu = 0; mu < D - 1; ++mu) {
+        const uint32_t xpmu = fwd(g, site, c[mu], mu);
+#pragma unroll 1
+        for (int nu = mu + 1; nu < D; ++nu) {
+            const uint32_t xpnu = fwd(g, site, c[nu], nu);
+            mat3<T> l, m, A, B, X;
+            T f[8];
+            load_link<T>(U, tix(site, D * 9, mu * 9), l);
+            load_link<T>(U, tix(xpmu, D * 9, nu * 9), m);
+            mul_nn(l, m, A); // a b
+            load_link<T>(U, tix(site, D * 9, nu * 9), l);
+            load_link<T>(U, tix(xpnu, D * 9, mu * 9), m);
+            mul_nn(l, m, B); // d c
+            im_tr_generators_of_product_na<T, false>(A, B, f);
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                fs[mu * 8 + a][t] += f[a];
+                fs[nu * 8 + a][t] -= f[a];
+            }
+            mul_na(m, A, X); // c A^dag
+            im_tr_generators_of_product<T, false>(X, l, f);
+            store_packed<8>(F, tix(xpnu, D * D * 8, mu * D * 8), md_slot<D>(nu, mu) * 8, f);
+            load_link<T>(U, tix(xpmu, D * 9, nu * 9), m);
+            mul_na(m, B, X); // b B^dag
+            load_link<T>(U, tix(site, D * 9, mu * 9), l);
+            im_tr_generators_of_product<T, false>(X, l, f);
+            store_packed<8>(F, tix(xpmu, D * D * 8, nu * D * 8), md_slot<D>(mu, nu) * 8, f);
+        }
+    }
+#pragma unroll
+    for (int mu = 0; mu < D; ++mu) {
+        T f[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) f[a] = fs[mu * 8 + a][t];
+        store_packed<8>(F, tix(site, D * D * 8, mu * D * 8), 0, f);
+    }
+}
+
+template <int D, typename T, bool COMP, int MODE>
+__global__ void __launch_bounds__(128) k_md_update(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout,
+                                                   const T *Ein, T *Eout, const T *__restrict__ F, Geo<D> g, T k1,
+                                                   T k2, T drift) {
+    static_assert(sizeof(T) == 8, "the split MD step is the FP64 state's");
+    static_assert(MODE & MD_KICK, "the force parts are summed for a kick");
+    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.x % D;
+    if (site >= g.V) return;
+    const size_t nt = tiles_of(g.V);
+    const size_t fi = tix(site, D * D * 8, mu * D * 8);
+    T f[8], p[8];
+    load_packed<8>(F, fi, 0, f);
+#pragma unroll
+    for (int k = 1; k < D; ++k) {
+        load_packed<8>(F, fi, k * 8, p);
+#pragma unroll
+        for (int a = 0; a < 8; ++a) f[a] += p[a];
+    }
+    mat3<T> u;
+    load_link<T>(Uin, tix(site, D * 9, mu * 9), u);
+    // the parts are twice the force (k_md_plaq leaves the projections' factor 1/2 out): halving the
+    // kick factors instead rounds the same
+    md_kick_drift<D, T, COMP, MODE>(f, u, Uin, Ein, Uout, Eout, Eout != Ein, site, mu, T(0.5) * k1, T(0.5) * k2,
+                                    drift, nt * D * 9 * kTile, nt * D * 8 * kTile);
 }
 
 // One projection sweep fused with the Gauss law of its result, one thread per site x:

@@ -109,6 +109,7 @@ void free_state(State *s) {
     if (s->E_alt) cudaFree(s->E_alt);
     if (s->G) cudaFree(s->G);
     if (s->G_alt) cudaFree(s->G_alt);
+    if (s->R) cudaFree(s->R);
     if (s->partial) cudaFree(s->partial);
     if (s->d_out) cudaFree(s->d_out);
     if (s->h_out) cudaFreeHost(s->h_out);
@@ -377,15 +378,21 @@ int project_gauss(State &s, int max_steps, int *steps_done) {
     const void *U = s.U[s.cur];
     uint32_t n = 0;
     int steps = 0;
-    LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+    if (fused) {
+        LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+    } else {
+        // FP64: the links' transport tables once, then every transport as a real 9x9 product
+        LQ_LAUNCH(s, LQ_KERNEL_OTHER, s.ops->adjoint_links(s, U));
+        LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss_adj(s, &n));
+    }
     for (;;) {
         if (fused) {
             LQ_LAUNCH(s, LQ_KERNEL_GAUSS_SWEEP, s.ops->gauss_sweep(s, U, &n));
             std::swap(s.E, s.E_alt);
             std::swap(s.G, s.G_alt);
         } else {
-            LQ_LAUNCH(s, LQ_KERNEL_GAUSS_SWEEP, s.ops->gauss_step(s, U));
-            LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss(s, U, &n));
+            LQ_LAUNCH(s, LQ_KERNEL_GAUSS_SWEEP, s.ops->gauss_step_adj(s));
+            LQ_LAUNCH(s, LQ_KERNEL_GAUSS, s.ops->gauss_adj(s, &n));
         }
         ++steps;
         if ((steps - 1) % 4 != 0) continue;
@@ -496,6 +503,7 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
     alloc(&s->E_alt, s->efield_bytes(), __LINE__);
     alloc(&s->G, s->gauss_bytes(), __LINE__);
     alloc(&s->G_alt, s->gauss_bytes(), __LINE__);
+    if (precision == LQ_PRECISION_F64) alloc(&s->R, s->adjoint_bytes(), __LINE__);
     alloc((void **)&s->partial, sizeof(double) * lq::kPartialRows * (size_t)s->partial_slots, __LINE__);
     alloc((void **)&s->d_out, sizeof(double) * 16, __LINE__);
     if (!rc) {
@@ -696,7 +704,8 @@ int lq_state_device_bytes(const lq_state *s, size_t *bytes) {
     LQ_CHECK_STATE(s);
     if (!bytes) return LQ_ERR_INVALID_ARGUMENT;
     *bytes = 3 * s->link_bytes() + 2 * s->efield_bytes() + 2 * s->gauss_bytes() +
-             sizeof(double) * (lq::kPartialRows * (size_t)s->partial_slots + 16) + s->staging_bytes;
+             sizeof(double) * (lq::kPartialRows * (size_t)s->partial_slots + 16) + s->staging_bytes +
+             (s->R ? s->adjoint_bytes() : 0);
     return LQ_OK;
 }
 

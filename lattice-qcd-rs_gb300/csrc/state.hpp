@@ -39,8 +39,11 @@ struct State {
     int cur = 0;
     void *E = nullptr;     // E-field (SoA)
     void *E_alt = nullptr; // second E buffer (projection sweeps are double-buffered)
-    void *G = nullptr;     // Gauss-law matrix G(x), Hermitian, 9 reals per site
+    void *G = nullptr;     // Gauss law G(x): Hermitian matrix, 9 reals per site (FP64 projection: components)
     void *G_alt = nullptr;
+    // FP64 scratch, 82 reals per link: the Gauss projection's transport tables of the links it
+    // projects on, and between projections the MD step's force parts (D x 8 reals per link)
+    void *R = nullptr;
     double *partial = nullptr;
     uint32_t partial_slots = 0; // slots per row of `partial`
     double *d_out = nullptr;    // device scalars
@@ -95,7 +98,9 @@ struct State {
     size_t link_bytes() const { return link_elems() * 2 * real_bytes * (comp ? 2 : 1); }
     size_t efield_elems() const { return padded_sites() * dim * 8; } // reals (hi part)
     size_t efield_bytes() const { return efield_elems() * real_bytes * (comp ? 2 : 1); }
-    size_t gauss_bytes() const { return padded_sites() * 9 * real_bytes; }
+    // G: 9 reals per site in the Hermitian form, 10 (9 components and a pad) in the FP64 projection's
+    size_t gauss_bytes() const { return padded_sites() * (precision == LQ_PRECISION_F64 ? 10 : 9) * real_bytes; }
+    size_t adjoint_bytes() const { return padded_sites() * dim * 82 * real_bytes; }
 };
 
 // Device operations of one (D, T, COMP) instantiation.  Launches are asynchronous on
@@ -119,6 +124,11 @@ struct Ops {
     // one projection step on E in place, from the G of the last gauss() call
     cudaError_t (*gauss_step)(State &s, const void *U);
     cudaError_t (*gauss_to_aos)(State &s, double *d_out);
+    // the FP64 projection in the adjoint representation (null for the FP32 forms): s.R <- the
+    // adjoint matrices of U; G <- the Gauss law's components and residual partials; one step on E
+    cudaError_t (*adjoint_links)(State &s, const void *U);
+    cudaError_t (*gauss_adj)(State &s, uint32_t *n_partials);
+    cudaError_t (*gauss_step_adj)(State &s);
     // plaquette partials (3 rows) of links buffer U, returns #partials
     cudaError_t (*plaquette)(State &s, const void *U, uint32_t *n_partials);
     // partials of sum Re Tr[P(Unew) - P(Uold)]

@@ -628,7 +628,38 @@ template <typename T> __device__ __forceinline__ void adj_mul(const T *c, const 
 
 // out^a = Im Tr(T^a a b) without forming the full product: only the imaginary parts of the
 // diagonal and the six off-diagonal entries of a b enter (90 multiply-adds instead of 108).
-template <typename T> __device__ __forceinline__ void im_tr_generators_of_product(const mat3<T> &a, const mat3<T> &b, T *out) {
+// out^a = Im Tr(T^a M) from the entries of M it needs: the off-diagonal pairs and the imaginary
+// parts of the diagonal
+template <typename T, bool HALF>
+__device__ __forceinline__ void im_tr_combine(const cpx<T> &m01, const cpx<T> &m10, const cpx<T> &m02,
+                                              const cpx<T> &m20, const cpx<T> &m12, const cpx<T> &m21, T i00, T i11,
+                                              T i22, T *out) {
+    if constexpr (HALF) {
+        const T h = T(0.5);
+        out[0] = h * (m10.im + m01.im);
+        out[1] = h * (m01.re - m10.re);
+        out[2] = h * (i00 - i11);
+        out[3] = h * (m20.im + m02.im);
+        out[4] = h * (m02.re - m20.re);
+        out[5] = h * (m21.im + m12.im);
+        out[6] = h * (m12.re - m21.re);
+        out[7] = T(kOneOver2Sqrt3) * (i00 + i11) + T(kMinusOneOverSqrt3) * i22;
+    } else {
+        out[0] = m10.im + m01.im;
+        out[1] = m01.re - m10.re;
+        out[2] = i00 - i11;
+        out[3] = m20.im + m02.im;
+        out[4] = m02.re - m20.re;
+        out[5] = m21.im + m12.im;
+        out[6] = m12.re - m21.re;
+        out[7] = T(2.0 * kOneOver2Sqrt3) * (i00 + i11) + T(2.0 * kMinusOneOverSqrt3) * i22;
+    }
+}
+
+// (HALF = false: twice the value, the factor 1/2 left to the caller -- a power of two, so applying it
+// later to a sum of such terms rounds exactly as applying it to each)
+template <typename T, bool HALF = true>
+__device__ __forceinline__ void im_tr_generators_of_product(const mat3<T> &a, const mat3<T> &b, T *out) {
     auto entry = [&](int i, int j) {
         T re = a.e[i * 3].re * b.e[j].re, im = a.e[i * 3].re * b.e[j].im;
         re = fma(-a.e[i * 3].im, b.e[j].im, re);
@@ -655,15 +686,116 @@ template <typename T> __device__ __forceinline__ void im_tr_generators_of_produc
     const cpx<T> m01 = entry(0, 1), m10 = entry(1, 0), m02 = entry(0, 2), m20 = entry(2, 0), m12 = entry(1, 2),
                  m21 = entry(2, 1);
     const T i00 = diag_im(0), i11 = diag_im(1), i22 = diag_im(2);
-    const T h = T(0.5);
-    out[0] = h * (m10.im + m01.im);
-    out[1] = h * (m01.re - m10.re);
-    out[2] = h * (i00 - i11);
-    out[3] = h * (m20.im + m02.im);
-    out[4] = h * (m02.re - m20.re);
-    out[5] = h * (m21.im + m12.im);
-    out[6] = h * (m12.re - m21.re);
-    out[7] = T(kOneOver2Sqrt3) * (i00 + i11) + T(kMinusOneOverSqrt3) * i22;
+    im_tr_combine<T, HALF>(m01, m10, m02, m20, m12, m21, i00, i11, i22, out);
+}
+
+// acc^a += k out^a, out^a = 2 Re Tr(T^a X Y) for traceless Hermitian X = x^c T^c, Y = y^d T^d from
+// their components: out^a = (1/2) d_acd x^c y^d, where Tr(T^a T^c T^d) = (d_acd + i f_acd) / 4 and the symmetric constants of
+// SU(3) in the Gell-Mann basis (adjoint_to_matrix's) are d_118 = d_228 = d_338 = -d_888 = 1/sqrt(3),
+// d_448 = d_558 = d_668 = d_778 = -1/(2 sqrt(3)), d_146 = d_157 = d_256 = d_344 = d_355 = 1/2,
+// d_247 = d_366 = d_377 = -1/2 (1-based indices; 58 multiply-adds instead of the matrix route's ~110)
+template <typename T>
+__device__ __forceinline__ void two_re_tr_generators_of_traceless_product(const T *x, const T *y, T k, T *acc) {
+    // acc^a += k out^a; the constants carry k (q = k/4, r = k/(2 sqrt(3)), s = k/(4 sqrt(3)))
+    const T q = k * T(0.25), r = k * T(kOneOver2Sqrt3), s = k * T(0.5 * kOneOver2Sqrt3);
+    auto pair = [&](int c, int d) { return fma(x[c], y[d], x[d] * y[c]); };
+    // 0-based: 1 -> 0, ..., 8 -> 7
+    {
+        T t = pair(3, 5);
+        t = fma(x[4], y[6], t);
+        t = fma(x[6], y[4], t);
+        acc[0] = fma(q, t, fma(r, pair(0, 7), acc[0]));
+    }
+    {
+        T t = pair(4, 5);
+        t = fma(-x[3], y[6], t);
+        t = fma(-x[6], y[3], t);
+        acc[1] = fma(q, t, fma(r, pair(1, 7), acc[1]));
+    }
+    {
+        T t = x[3] * y[3];
+        t = fma(x[4], y[4], t);
+        t = fma(-x[5], y[5], t);
+        t = fma(-x[6], y[6], t);
+        acc[2] = fma(q, t, fma(r, pair(2, 7), acc[2]));
+    }
+    {
+        T t = pair(0, 5);
+        t = fma(-x[1], y[6], t);
+        t = fma(-x[6], y[1], t);
+        t = fma(x[2], y[3], t);
+        t = fma(x[3], y[2], t);
+        acc[3] = fma(q, t, fma(-s, pair(3, 7), acc[3]));
+    }
+    {
+        T t = pair(0, 6);
+        t = fma(x[1], y[5], t);
+        t = fma(x[5], y[1], t);
+        t = fma(x[2], y[4], t);
+        t = fma(x[4], y[2], t);
+        acc[4] = fma(q, t, fma(-s, pair(4, 7), acc[4]));
+    }
+    {
+        T t = pair(0, 3);
+        t = fma(x[1], y[4], t);
+        t = fma(x[4], y[1], t);
+        t = fma(-x[2], y[5], t);
+        t = fma(-x[5], y[2], t);
+        acc[5] = fma(q, t, fma(-s, pair(5, 7), acc[5]));
+    }
+    {
+        T t = pair(0, 4);
+        t = fma(-x[1], y[3], t);
+        t = fma(-x[3], y[1], t);
+        t = fma(-x[2], y[6], t);
+        t = fma(-x[6], y[2], t);
+        acc[6] = fma(q, t, fma(-s, pair(6, 7), acc[6]));
+    }
+    {
+        T a = x[0] * y[0];
+        a = fma(x[1], y[1], a);
+        a = fma(x[2], y[2], a);
+        a = fma(-x[7], y[7], a);
+        T b = x[3] * y[3];
+        b = fma(x[4], y[4], b);
+        b = fma(x[5], y[5], b);
+        b = fma(x[6], y[6], b);
+        acc[7] = fma(r, a, fma(-s, b, acc[7]));
+    }
+}
+
+// out^a = Im Tr(T^a a b^dagger) without forming the product: the imaginary parts of the diagonal and the
+// six off-diagonal entries of a b^dagger, (a b^dagger)_ij = sum_k a_ik conj(b_jk), in mul_na's order
+template <typename T, bool HALF = true>
+__device__ __forceinline__ void im_tr_generators_of_product_na(const mat3<T> &a, const mat3<T> &b, T *out) {
+    auto entry = [&](int i, int j) {
+        T re = a.e[i * 3].re * b.e[j * 3].re;
+        T im = -a.e[i * 3].re * b.e[j * 3].im;
+        re = fma(a.e[i * 3].im, b.e[j * 3].im, re);
+        im = fma(a.e[i * 3].im, b.e[j * 3].re, im);
+#pragma unroll
+        for (int k = 1; k < 3; ++k) {
+            re = fma(a.e[i * 3 + k].re, b.e[j * 3 + k].re, re);
+            re = fma(a.e[i * 3 + k].im, b.e[j * 3 + k].im, re);
+            im = fma(-a.e[i * 3 + k].re, b.e[j * 3 + k].im, im);
+            im = fma(a.e[i * 3 + k].im, b.e[j * 3 + k].re, im);
+        }
+        return cmk(re, im);
+    };
+    auto diag_im = [&](int i) {
+        T im = -a.e[i * 3].re * b.e[i * 3].im;
+        im = fma(a.e[i * 3].im, b.e[i * 3].re, im);
+#pragma unroll
+        for (int k = 1; k < 3; ++k) {
+            im = fma(-a.e[i * 3 + k].re, b.e[i * 3 + k].im, im);
+            im = fma(a.e[i * 3 + k].im, b.e[i * 3 + k].re, im);
+        }
+        return im;
+    };
+    const cpx<T> m01 = entry(0, 1), m10 = entry(1, 0), m02 = entry(0, 2), m20 = entry(2, 0), m12 = entry(1, 2),
+                 m21 = entry(2, 1);
+    const T i00 = diag_im(0), i11 = diag_im(1), i22 = diag_im(2);
+    im_tr_combine<T, HALF>(m01, m10, m02, m20, m12, m21, i00, i11, i22, out);
 }
 
 } // namespace lq

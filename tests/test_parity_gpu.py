@@ -149,6 +149,23 @@ def test_project_to_gauss(oracle_mod, lqgpu_mod, dim, L):
         assert rel(s.e_field(), e_ref) <= TOL
 
 
+@pytest.mark.parametrize("dim,L", [(3, 4), (4, 4)])
+def test_project_to_gauss_links_off_the_group(oracle_mod, lqgpu_mod, dim, L):
+    """Links that are not exactly unitary (the leap-frog's first-order link update leaves
+    |U U^dag - 1| ~ 1e-8 after a trajectory) enter the projection's parallel transports as full
+    matrices: U^dag E U then has a trace, and G(x) with it (src/field.rs:1174-1195)."""
+    O, G = oracle_mod, lqgpu_mod
+    links, e = random_fields(O, dim, L, 23)
+    links = links * (1.0 + 1e-6 * np.random.default_rng(5).standard_normal(links.shape))
+    e_ref, steps_ref = O.project_to_gauss(dim, L, links, e)
+    with G.State(dim, L, 1000.0, 1.0, G.PRECISION_F64) as s:
+        s.set_link_matrix(links)
+        s.set_e_field(e)
+        steps = s.project_to_gauss()
+        assert steps == steps_ref
+        assert rel(s.e_field(), e_ref) <= TOL
+
+
 def test_normalize(oracle_mod, lqgpu_mod):
     O, G = oracle_mod, lqgpu_mod
     dim, L = 4, 3

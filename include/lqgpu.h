@@ -118,12 +118,11 @@ int lq_state_save(lq_state *s, void *buf, size_t n_bytes);
 int lq_state_load(const void *buf, size_t n_bytes, lq_state **out);
 /* Attach a cudaStream_t (passed as void*); NULL selects the legacy default stream. */
 int lq_state_set_stream(lq_state *s, void *cuda_stream);
-/* The Gauss projection's sweep loop (EField::project_to_gauss, src/field.rs:1265-1294) of the
- * FP32-arithmetic forms runs as one CUDA graph launch whose convergence test is a device kernel
- * driving a conditional while node (enable = 1, the default), or as host-driven launches with
- * one host read of the residual per test (enable = 0).  Both give the same sweeps and the same
- * field; the FP64 form always uses host-driven launches.  A driver that cannot build the graph
- * turns it off for the state.  Without a step limit (max_steps <= 0) the graph's device-side loop
+/* The Gauss projection's sweep loop (EField::project_to_gauss, src/field.rs:1265-1294) runs as
+ * one CUDA graph launch whose convergence test is a device kernel driving a conditional while node
+ * (enable = 1, the default), or as host-driven launches with one host read of the residual per
+ * test (enable = 0).  Both give the same sweeps and the same field.  A driver that cannot build
+ * the graph turns it off for the state.  Without a step limit (max_steps <= 0) the graph's device-side loop
  * still stops after 10001 sweeps with LQ_ERR_NOT_CONVERGED, the limit of a batch's loop too. */
 int lq_state_set_projection_graph(lq_state *s, int enable);
 /* Getters: LatticeCyclic::dim/size, LatticeState::beta, LatticeStateWithEField::t,

@@ -249,7 +249,14 @@ int capture_projection(State &s, int max_steps, cudaGraphExec_t *out) {
     bool capturing = e == cudaSuccess;
     cudaGraphConditionalHandle h = 0;
     uint32_t n = 0;
+    // FP32 forms: one fused sweep, double-buffered; FP64: the step in place and the Gauss law on the
+    // links' transport tables
+    const bool fused = s.precision != LQ_PRECISION_F64;
     auto sweep = [&]() {
+        if (!fused) {
+            cudaError_t r = s.ops->gauss_step_adj(s);
+            return r == cudaSuccess ? s.ops->gauss_adj(s, &n) : r;
+        }
         cudaError_t r = s.ops->gauss_sweep(s, U, &n);
         std::swap(s.E, s.E_alt);
         std::swap(s.G, s.G_alt);
@@ -261,7 +268,8 @@ int capture_projection(State &s, int max_steps, cudaGraphExec_t *out) {
     }
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.d_proj, 0, 4 * sizeof(int), s.stream);
-    if (e == cudaSuccess) e = s.ops->gauss(s, U, &n);
+    if (e == cudaSuccess) e = fused ? s.ops->gauss(s, U, &n) : s.ops->adjoint_links(s, U);
+    if (e == cudaSuccess && !fused) e = s.ops->gauss_adj(s, &n);
     if (e == cudaSuccess) e = sweep();
     if (e == cudaSuccess) {
         k_proj_check<<<1, 1024, 0, s.stream>>>(s.partial, n, threshold, 1, max_steps, s.d_proj, h);
@@ -343,15 +351,20 @@ int project_gauss_graph(State &s, int max_steps, int *steps_done) {
     const cudaError_t e = cudaGraphLaunch(exec, s.stream);
     prof_end(s, slot, LQ_KERNEL_GAUSS_SWEEP);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch (projection)", __LINE__);
-    // 1 + 4k sweeps: E and G end in the other buffers
-    std::swap(s.E, s.E_alt);
-    std::swap(s.G, s.G_alt);
+    const bool fused = s.precision != LQ_PRECISION_F64;
+    // fused sweeps: 1 + 4k of them leave E and G in the other buffers
+    if (fused) {
+        std::swap(s.E, s.E_alt);
+        std::swap(s.G, s.G_alt);
+    }
     LQ_CK(cudaMemcpyAsync(s.h_out, s.d_proj, 2 * sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     LQ_CK(cudaStreamSynchronize(s.stream));
     int ctl[2];
     memcpy(ctl, s.h_out, sizeof(ctl));
-    // the slot covers the Gauss law, the sweeps and the tests
-    if (s.prof && slot >= 0) s.prof->cnt[slot] = 1 + ctl[0] + (ctl[0] + 3) / 4;
+    // the slot covers the Gauss law, the sweeps (FP64: a step and a Gauss law each, after the
+    // transport tables) and the tests
+    if (s.prof && slot >= 0)
+        s.prof->cnt[slot] = fused ? 1 + ctl[0] + (ctl[0] + 3) / 4 : 2 + 2 * ctl[0] + (ctl[0] + 3) / 4;
     prof_flush(s);
     if (steps_done) *steps_done = ctl[0];
     if (ctl[1] != LQ_OK) return ctl[1];
@@ -370,7 +383,7 @@ int project_gauss(State &s, int max_steps, int *steps_done) {
     // FP32 arithmetic: one fused sweep per step (U read once).  FP64: the step and the Gauss
     // law as two kernels, since the sweep's recomputed neighbour updates cost FP64 flops.
     const bool fused = s.precision != LQ_PRECISION_F64;
-    if (fused && s.proj_graph) {
+    if (s.proj_graph) {
         const int rc = project_gauss_graph(s, max_steps, steps_done);
         if (rc != -1) return rc;
     }

@@ -59,9 +59,10 @@ struct State {
     int prefetch_pending = 0;
 
     // the Gauss projection's sweep loop as a CUDA graph whose while node the device-side check
-    // drives (lq_state_set_projection_graph; FP32 arithmetic forms): one instantiation per
-    // (link buffer, E buffer order, G buffer order, step limit) met, built on first use; 12 entries
-    // hold every combination of the 3 link buffers and 2 x 2 buffer orders (an HMC loop meets 6)
+    // drives (lq_state_set_projection_graph): one instantiation per (link buffer, E buffer order,
+    // G buffer order, step limit) met, built on first use; 12 entries hold every combination of the
+    // 3 link buffers and 2 x 2 buffer orders (an HMC loop meets 6; the FP64 form, whose sweeps work in
+    // place, 3)
     struct ProjGraph {
         const void *U;
         const void *E;

@@ -2,7 +2,8 @@
 convergence test) against the host-driven loop (one host read of the residual per test): the same
 number of sweeps, bitwise the same projected field and Gauss law, the same errors at the step limit
 and on a non-finite field, and the same trajectories while the graph cache meets every link buffer
-and E/G buffer order of a state.  FP32-arithmetic forms (the FP64 form always uses the host loop)."""
+and E/G buffer order of a state.  Every form: the FP32-arithmetic ones sweep with one fused kernel on
+double-buffered fields, the FP64 one with its step and Gauss-law kernels in place."""
 import numpy as np
 import pytest
 
@@ -20,7 +21,7 @@ def pair(G, precision, seed=3):
     return a, b
 
 
-@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("precision", [1, 2, 0])
 def test_projection_graph_equals_host_loop(lqgpu_mod, precision):
     G = lqgpu_mod
     a, b = pair(G, precision)
@@ -42,7 +43,7 @@ def test_projection_graph_equals_host_loop(lqgpu_mod, precision):
             assert np.array_equal(a.link_matrix(), b.link_matrix())
 
 
-@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("precision", [1, 2, 0])
 def test_projection_graph_trajectories(lqgpu_mod, precision):
     G = lqgpu_mod
     a, b = pair(G, precision, seed=8)
@@ -56,7 +57,7 @@ def test_projection_graph_trajectories(lqgpu_mod, precision):
         assert np.array_equal(a.e_field(), b.e_field())
 
 
-@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("precision", [1, 2, 0])
 def test_projection_graph_errors(lqgpu_mod, precision):
     G = lqgpu_mod
     a, b = pair(G, precision)
@@ -89,7 +90,7 @@ def test_projection_graph_errors(lqgpu_mod, precision):
         assert np.array_equal(a.e_field(), b.e_field())
 
 
-@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("precision", [1, 2, 0])
 def test_projection_graph_without_step_limit(lqgpu_mod, precision):
     """max_steps <= 0: the host loop has no limit, the graph its own bound; a field that converges
     gives the same sweeps and field either way."""
@@ -119,15 +120,18 @@ def test_projection_graph_tiny_lattices(lqgpu_mod, dim, Lt):
         assert np.array_equal(a.link_matrix(), b.link_matrix())
 
 
-def test_projection_graph_profile_counts(lqgpu_mod):
-    """The graph's profile slot counts the Gauss law, every sweep and every test."""
+@pytest.mark.parametrize("precision", [1, 0])
+def test_projection_graph_profile_counts(lqgpu_mod, precision):
+    """The graph's profile slot counts the Gauss law, every sweep and every test (FP64: the transport
+    tables, the first Gauss law, then a step and a Gauss law per sweep)."""
     G = lqgpu_mod
-    with G.State(DIM, L, SIZE, BETA, G.PRECISION_MIXED) as s:
+    with G.State(DIM, L, SIZE, BETA, precision) as s:
         s.set_links_random(2)
         s.set_e_field_normal(4, 0, 0.25)
         s.profile_enable(True)
         s.profile_read(reset=True)
         steps = s.project_to_gauss()
         prof = s.profile_read(reset=True)
-        assert prof["gauss_sweep"][0] == 1 + steps + (steps + 3) // 4
+        kernels = 1 + steps if precision else 2 + 2 * steps
+        assert prof["gauss_sweep"][0] == kernels + (steps + 3) // 4
         assert prof["gauss_sweep"][1] > 0.0

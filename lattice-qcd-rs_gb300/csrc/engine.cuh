@@ -71,7 +71,7 @@ template <int D, typename T, bool COMP> struct Engine {
                 (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, (const T *)s.R, geo(s), k1, k2, drift);
         } else if constexpr (MdSite<T>::on && (M & MD_KICK)) {
             k_md_site<D, T, COMP, M><<<(s.V + kMdSiteBlock - 1) / kMdSiteBlock, kMdSiteBlock, 0, s.stream>>>(
-                (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, geo(s), k1, k2, drift);
+                (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, geo(s), k1, k2, drift, s.block_order);
         } else {
             k_md<D, T, COMP, M><<<md_grid_k(s), md_block_k(), 0, s.stream>>>(
                 (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, geo(s), k1, k2, drift);
@@ -129,7 +129,8 @@ template <int D, typename T, bool COMP> struct Engine {
     static cudaError_t gauss_sweep(State &s, const void *U, uint32_t *n_partials) {
         const uint32_t blocks = (s.V + 127) / 128;
         k_gauss_sweep<D, T, false><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.E_alt,
-                                                                  (const T *)s.G, (T *)s.G_alt, geo(s), s.partial);
+                                                                  (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
+                                                                  s.block_order);
         *n_partials = blocks;
         return cudaGetLastError();
     }

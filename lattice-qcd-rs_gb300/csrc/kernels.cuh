@@ -14,6 +14,7 @@
 // +-mu neighbour of a site is +-L^mu with periodic wrap.  Arrays are padded to whole tiles;
 // padded sites are never written by the kernels and stay zero.
 #pragma once
+#include "block_order.hpp"
 #include "su3.cuh"
 
 namespace lq {
@@ -467,10 +468,10 @@ __device__ __forceinline__ void md_site(const V2<T> *__restrict__ Uin, V2<T> *__
 template <int D, typename T, bool COMP, int MODE>
 __global__ void __launch_bounds__(kMdSiteBlock, MinBlocks<T>::md_site)
     k_md_site(const V2<T> *__restrict__ Uin, V2<T> *__restrict__ Uout, const T *Ein, T *Eout, Geo<D> g, T k1, T k2,
-              T drift) {
+              T drift, BlockOrder bo) {
     // the parts of later directions' forces from the planes (mu, nu > mu), one column per thread
     __shared__ T fs[(D - 1) * 8][kMdSiteBlock];
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t site = block_at(bo, blockIdx.x) * blockDim.x + threadIdx.x;
     if (site >= g.V) return;
     const size_t nt = tiles_of(g.V);
     md_site<D, T, COMP, MODE>(Uin, Uout, Ein, Eout, g, site, k1, k2, drift, nt * D * 9 * kTile, nt * D * 8 * kTile, fs,
@@ -1025,12 +1026,14 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
 template <int D, typename T, bool COMP>
 __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                                      T *__restrict__ Eout, const T *__restrict__ Gin,
-                                                     T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial) {
-    const uint32_t site = blockIdx.x * blockDim.x + threadIdx.x;
+                                                     T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial,
+                                                     BlockOrder bo) {
+    const uint32_t blk = block_at(bo, blockIdx.x); // the residual partial keeps its site-order slot
+    const uint32_t site = blk * blockDim.x + threadIdx.x;
     double r[1] = {0.0};
     if (site < g.V)
         r[0] = sweep_site<D, T, COMP>(U, Ein, Eout, Gin, Gout, g, site, (size_t)tiles_of(g.V) * D * 8 * kTile);
-    block_reduce_store<1>(r, partial, blockIdx.x, gridDim.x);
+    block_reduce_store<1>(r, partial, blk, gridDim.x);
 }
 
 // ------------------------------------------------------------------ plaquettes

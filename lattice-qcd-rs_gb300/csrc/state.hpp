@@ -5,6 +5,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "block_order.hpp"
 #include "lqgpu.h"
 
 namespace lq {
@@ -92,6 +93,8 @@ struct State {
 
     const Ops *ops = nullptr;
     Prof *prof = nullptr; // non-null while profiling is enabled
+    // launch order of the per-site stencil kernels' blocks (block_order.hpp)
+    BlockOrder block_order = {0, 1, 1, 1};
 
     // arrays are stored in tiles of 32 sites (padded; see tix() in su3.cuh)
     size_t padded_sites() const { return ((size_t)V + 31) / 32 * 32; }

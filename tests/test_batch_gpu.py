@@ -190,19 +190,20 @@ def test_eager_kernel_profile_counts_every_launch(lqgpu_mod):
         b.profile_enable(False)
 
 
-@pytest.mark.parametrize("dim", [2, 3, 4])
-def test_lone_state_at_L32_equals_batched_ensemble(lqgpu_mod, dim):
+@pytest.mark.parametrize("dim,L", [(2, 32), (3, 32), (4, 32), (4, 48)])
+def test_lone_state_at_L32_equals_batched_ensemble(lqgpu_mod, dim, L):
     """the headline's side length: a lone mixed state and the same lattice as a one-ensemble batch
     (the batch's persistent kernels over a chunk table) give the same accept decisions, projection
-    steps and links, bitwise"""
+    steps and links, bitwise.  At 48^4 the lone state's MD and sweep kernels visit their blocks in
+    strips (block_order.hpp) while the batch's run in site order."""
     G = lqgpu_mod
-    with G.Batch(dim, [32], [1000.0], [2.0], G.PRECISION_MIXED) as b:
+    with G.Batch(dim, [L], [1000.0], [2.0], G.PRECISION_MIXED) as b:
         b.set_links_random(LINK_SEED)
         b.set_seed(SEED, 0)
         b.hmc_run(DT, 3, 2, MAXG)
         rb = b.hmc_results()
         links_b = b.link_matrix(0)
-    with G.State(dim, 32, 1000.0, 2.0, G.PRECISION_MIXED) as s:
+    with G.State(dim, L, 1000.0, 2.0, G.PRECISION_MIXED) as s:
         s.set_links_random(LINK_SEED)
         for k in range(2):
             r = s.hmc_trajectory(DT, 3, SEED, k, float(rb["uniform"][k, 0]))

@@ -18,6 +18,10 @@
 
 using lq::State;
 
+#ifndef LQ_BLOCK_REUSE_SITES
+#define LQ_BLOCK_REUSE_SITES 32768
+#endif
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -503,9 +507,10 @@ int lq_state_create(int dim, int L, double size, double beta, int precision, lq_
     s->ops = precision == LQ_PRECISION_F64 ? lq::ops_f64(dim)
              : precision == LQ_PRECISION_MIXED ? lq::ops_mixed(dim)
                                                : lq::ops_f32(dim);
-    // strips keep a neighbour along the slowest direction within about 32768 sites of work, under half
-    // of what the resident blocks of the stencil kernels cover at once (152 SMs x 4 blocks x 128 sites)
-    s->block_order = lq::make_block_order(dim, (uint32_t)L, 128, 32768);
+    // strips keep a neighbour along the slowest direction within LQ_BLOCK_REUSE_SITES sites of work,
+    // under half of what the resident blocks of the stencil kernels cover at once (152 SMs x 4 blocks
+    // x 128 sites)
+    s->block_order = lq::make_block_order(dim, (uint32_t)L, 128, LQ_BLOCK_REUSE_SITES);
     s->partial_slots = lq::partial_slots_for(s->V);
     if (s->partial_slots < 1024) s->partial_slots = 1024;
     int rc = LQ_OK;

@@ -134,11 +134,6 @@ template <int D, typename T, bool COMP> struct Engine {
         *n_partials = blocks;
         return cudaGetLastError();
     }
-    static cudaError_t gauss_step(State &s, const void *U) {
-        const dim3 grid(((s.V + 127) / 128) * D, 1, 1);
-        k_gauss_step<D, T, COMP><<<grid, 128, 0, s.stream>>>((const V2<T> *)U, (T *)s.E, (const T *)s.G, geo(s));
-        return cudaGetLastError();
-    }
     static constexpr bool kAdjointProjection = std::is_same<T, double>::value;
     static cudaError_t adjoint_links(State &s, const void *U) {
         if constexpr (kAdjointProjection) {
@@ -280,7 +275,7 @@ template <int D, typename T, bool COMP> struct Engine {
     static const Ops *table() {
         static const Ops ops = {links_from_aos, links_to_aos,  links_cold,      links_random, efield_from_aos,
                                 efield_to_aos,  efield_normal, md,              gauss,        gauss_sweep,
-                                gauss_step,     gauss_to_aos,
+                                gauss_to_aos,
                                 kAdjointProjection ? adjoint_links : nullptr,
                                 kAdjointProjection ? gauss_adj : nullptr,
                                 kAdjointProjection ? gauss_step_adj : nullptr,

@@ -609,35 +609,6 @@ __device__ __forceinline__ void projection_step(const mat3<T> &u, const mat3<T> 
     }
 }
 
-// One projection step on every link with G precomputed by k_gauss (the unfused form, used by
-// the FP64 state, whose arithmetic rate makes the sweep's recomputation too costly).  E is
-// updated in place: each thread reads and writes only its own link.
-template <int D, typename T, bool COMP>
-__global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U, T *__restrict__ E,
-                                                    const T *__restrict__ G, Geo<D> g) {
-    const uint32_t site = (blockIdx.x / D) * blockDim.x + threadIdx.x;
-    const int mu = blockIdx.x % D;
-    if (site >= g.V) return;
-    const size_t elo = (size_t)tiles_of(g.V) * D * 8 * kTile;
-    uint32_t c[D];
-    site_coords(g, site, c);
-    mat3<T> u, gx, gp;
-    herm_load(G, site, gx);
-    herm_load(G, fwd(g, site, c[mu], mu), gp);
-    load_link<T>(U, tix(site, D * 9, mu * 9), u);
-    const size_t ei = tix(site, D * 8, mu * 8);
-    T gxc[8], e[8], el[8];
-    two_re_tr_generators(gx, gxc);
-    load_efield<T>(E, ei, e);
-    if (COMP) load_efield<T>(E + elo, ei, el);
-    else
-#pragma unroll
-        for (int a = 0; a < 8; ++a) el[a] = T(0);
-    projection_step<T, COMP>(u, gx, gxc, gp, e, el);
-    store_efield<T>(E, ei, e);
-    if (COMP) store_efield<T>(E + elo, ei, el);
-}
-
 // ---- the FP64 projection in the adjoint representation ----
 // The projection changes E only: its links are fixed.  So the maps X -> U X U^dag and
 // X -> U^dag X U of every link on Hermitian 3x3 matrices are formed once per projection
@@ -651,8 +622,8 @@ __global__ void __launch_bounds__(128) k_gauss_step(const V2<T> *__restrict__ U,
 //   A_a = 2 Re Tr(T^a U U^dag),  B_a = 2 Re Tr(T^a U^dag U),  t = Tr(U U^dag)
 //   U X U^dag:  y^a = R_ab x^b + A_a x^8 / 3,   y^8 = B_b x^b / 2 + t x^8 / 3
 //   U^dag X U:  y^a = R_ba x^b + B_a x^8 / 3,   y^8 = A_b x^b / 2 + t x^8 / 3
-// The arithmetic is k_gauss / k_gauss_step's up to rounding: the FP64 state's projection, bound
-// by its FP64 multiply-add rate.
+// The arithmetic is that of the matrix-form step (projection_step) and Gauss law (k_gauss) up to
+// rounding: the FP64 state's projection, bound by its FP64 multiply-add rate.
 //
 // Layout of the table: the kAdjReals reals of the link (site, mu) fill planes mu*kAdjReals ..
 // of a tile (tix(site, D * kAdjReals, mu * kAdjReals)): R row-major, A, B, t and one pad, packed in
@@ -681,8 +652,7 @@ __device__ __forceinline__ void store_packed(double *__restrict__ A, size_t idx,
     for (int j = 0; j < N / 2; ++j) q[(first / 2 + j) * kTile] = make_double2(v[2 * j], v[2 * j + 1]);
 }
 
-// the transport table of every link, one thread per link (directions fastest in the block order, as
-// k_gauss_step).  Row a of R holds the generator components of Q^a = U^dag T^a U, whose entries are
+// the transport table of every link, one thread per link (directions fastest in the block order).  Row a of R holds the generator components of Q^a = U^dag T^a U, whose entries are
 // sums of P^{rc}_ij = conj(U_ri) U_cj over the nonzero entries (r, c) of T^a (adjoint_to_matrix's
 // Gell-Mann basis): with S = P^{rc} + P^{cr} and A = P^{cr} - P^{rc},
 //   (r, c) = (0, 1): Q^0 = S / 2, Q^1 = i A / 2;  (0, 2): Q^3, Q^4;  (1, 2): Q^5, Q^6 likewise;
@@ -807,7 +777,7 @@ __global__ void __launch_bounds__(256) k_gauss_adj(const T *__restrict__ R, cons
     block_reduce_store<1>(res, partial, blockIdx.x, gridDim.x);
 }
 
-// One projection step on every link from the components of G (k_gauss_step's arithmetic):
+// One projection step on every link from the components of G (projection_step's arithmetic):
 //   e^a += 0.12 (2 Re Tr(T^a H G(x+mu)) - 2 Re Tr(T^a G(x))),  H = U G(x) U^dag
 // with 2 Re Tr(T^a H P) = 2 Re Tr(T^a H0 P0) + h^8 p^a / 3 + p^8 h^a / 3 for H0, P0 the
 // traceless parts; the factor 0.12 rides on the constants of each term.

@@ -125,8 +125,6 @@ struct Ops {
     cudaError_t (*gauss)(State &s, const void *U, uint32_t *n_partials);
     // one projection sweep E -> E_alt with G -> G_alt (= gauss(E_alt)) and its residual partials
     cudaError_t (*gauss_sweep)(State &s, const void *U, uint32_t *n_partials);
-    // one projection step on E in place, from the G of the last gauss() call
-    cudaError_t (*gauss_step)(State &s, const void *U);
     cudaError_t (*gauss_to_aos)(State &s, double *d_out);
     // the FP64 projection in the adjoint representation (null for the FP32 forms): s.R <- the
     // adjoint matrices of U; G <- the Gauss law's components and residual partials; one step on E

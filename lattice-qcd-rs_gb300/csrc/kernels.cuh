@@ -401,8 +401,8 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::md) k_md(const V2<T> *__res
 // U_mu(x) U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag: U_mu(x) S+_mu,nu(x) = P and U_nu(x) S+_nu,mu(x) =
 // P^dag, so Im Tr(T^a .) of one product serves both links with opposite signs.  Per site the forward
 // staples then cost D(D-1)/2 plaquettes (two products and one projected product each) instead of
-// D(D-1) staples of two products and their share of U Sigma: 4788 multiply-add-sized steps per site
-// at D = 4 instead of 5544.  The backward staples keep staple_sum's products.  Each link's force
+// D(D-1) staples of two products each: 1964 instructions per link against 2200 for k_md (mixed, D = 4,
+// ncu).  The backward staples keep staple_sum's products.  Each link's force
 // is complete once the planes (mu, nu > mu) and (nu < mu, mu) and its backward staples are summed,
 // and that link is kicked and drifted by md_update's arithmetic before the next direction.  The
 // force is summed per plaquette rather than as one staple matrix, so the results differ from k_md's

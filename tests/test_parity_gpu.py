@@ -107,6 +107,29 @@ def test_integrate_sync_modes(oracle_mod, lqgpu_mod, dim, L, mode, n):
         assert s.t == n
 
 
+@pytest.mark.parametrize("dim", [2, 3, 4])
+@pytest.mark.parametrize("mode,n", [(4, 3), (0, 2)])
+def test_smallest_lattice_wraps(oracle_mod, lqgpu_mod, dim, mode, n):
+    """L = 2: x + mu and x - mu are the same site, so each plaquette meets the wrap-around in all its
+    links, and the FP64 MD step's force parts for a link arrive from a site that is both its forward
+    and its backward neighbour; the projection on the same fields too."""
+    O, G = oracle_mod, lqgpu_mod
+    size, dt, L = 7.0, 0.05, 2
+    links, e = random_fields(O, dim, L, 31)
+    lr, er = O.integrate(dim, L, size, links, e, mode, dt, n)
+    e_ref, steps_ref = O.project_to_gauss(dim, L, links, e)
+    with G.State(dim, L, size, 1.0, G.PRECISION_F64) as s:
+        s.set_link_matrix(links)
+        s.set_e_field(e)
+        s.integrate(mode, dt, n)
+        assert rel(s.link_matrix(), lr) <= TOL
+        assert rel(s.e_field(), er) <= TOL
+        s.set_link_matrix(links)
+        s.set_e_field(e)
+        assert s.project_to_gauss() == steps_ref
+        assert rel(s.e_field(), e_ref) <= TOL
+
+
 @pytest.mark.parametrize("dim,L", [(2, 4), (3, 3), (4, 3)])
 def test_leapfrog_chain(oracle_mod, lqgpu_mod, dim, L):
     """sync_leap, leap_leap x2, leap_sync and simulate_using_leapfrog_n"""

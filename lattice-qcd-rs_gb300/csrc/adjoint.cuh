@@ -47,12 +47,44 @@ __global__ void __launch_bounds__(128) k_adj_init(const V2<T> *__restrict__ U, V
     store_link<T>(lamU, tix(site, D * 9, mu * 9), r);
 }
 
+// r += (NEG ? -1 : 1) p W for W = sum_a c^a T^a (Hermitian traceless: real diagonal, lower
+// off-diagonal entries the conjugates of the upper ones), multiplied from the right
+template <typename T, bool NEG>
+__device__ __forceinline__ void mul_adj_acc(const mat3<T> &p, const T *c, mat3<T> &r) {
+    const T h = T(0.5);
+    const T c8p = T(kOneOver2Sqrt3) * c[7];
+    const T d[3] = {h * c[2] + c8p, -h * c[2] + c8p, T(kMinusOneOverSqrt3) * c[7]};
+    const cpx<T> e01 = cmk(h * c[0], -h * c[1]), e02 = cmk(h * c[3], -h * c[4]), e12 = cmk(h * c[5], -h * c[6]);
+    // W by columns: W_kj for k = 0, 1, 2
+    const cpx<T> w[3][3] = {{cmk(d[0], T(0)), cmk(e01.re, -e01.im), cmk(e02.re, -e02.im)},
+                            {e01, cmk(d[1], T(0)), cmk(e12.re, -e12.im)},
+                            {e02, e12, cmk(d[2], T(0))}};
+    const T sg = NEG ? T(-1) : T(1);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            T re = r.e[i * 3 + j].re, im = r.e[i * 3 + j].im;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const cpx<T> a = p.e[i * 3 + k], b = w[j][k];
+                re = fma(sg * a.re, b.re, re);
+                im = fma(sg * a.re, b.im, im);
+                if (k != j) { // the diagonal of W is real
+                    re = fma(-sg * a.im, b.im, re);
+                }
+                im = fma(sg * a.im, b.re, im);
+            }
+            r.e[i * 3 + j] = cmk(re, im);
+        }
+}
+
 // one plaquette loop U_m X Y Z of link m: R of the loop (see the header comment).  Each of X,
 // Y, Z is link `l` traversed forward (fwd = true: U_l) or backward (U_l^dag); cl: lam_E of l.
 template <typename T>
 __device__ __forceinline__ void loop_r(const mat3<T> (&u)[3], const T (&cl)[3][8], const bool (&fwd)[3],
                                        const mat3<T> &wm, mat3<T> &racc) {
-    mat3<T> p, q, t, d;
+    mat3<T> p, q, t;
     // the first factor
     if (fwd[0]) {
         p = u[0];
@@ -64,23 +96,21 @@ __device__ __forceinline__ void loop_r(const mat3<T> (&u)[3], const T (&cl)[3][8
 #pragma unroll
         for (int k = 0; k < 9; ++k) q.e[k] = cmk(-q.e[k].re, -q.e[k].im);
     }
+    // the product and its single-insertion sum through the next factors as a pair (p, q):
+    //   forward U:   (p U, q U + p W U) = (p U, (q + p W) U)
+    //   backward U^dag, inserted as -U^dag W:   (p U^dag, q U^dag - (p U^dag) W)
+    // one product fewer per factor than forming W U and p (W U) apart
 #pragma unroll
     for (int f = 1; f < 3; ++f) {
         mat3<T> np, nq;
         if (fwd[f]) {
             mul_nn(p, u[f], np);
+            mul_adj_acc<T, false>(p, cl[f], q); // q + p W
             mul_nn(q, u[f], nq);
-            adj_mul<T>(cl[f], u[f], d); // W U
-            mat3<T> pd;
-            mul_nn(p, d, pd);
-            mat_axpy(T(1), pd, nq);
         } else {
             mul_na(p, u[f], np);
             mul_na(q, u[f], nq);
-            adj_mul<T>(cl[f], u[f], d); // W U; the factor is -(W U)^dag
-            mat3<T> pd;
-            mul_na(p, d, pd);
-            mat_axpy(T(-1), pd, nq);
+            mul_adj_acc<T, true>(np, cl[f], nq);
         }
         p = np;
         q = nq;

@@ -128,9 +128,17 @@ template <int D, typename T, bool COMP> struct Engine {
     // (both Hamiltonians see the same start); the caller clears the lo parts afterwards.
     static cudaError_t gauss_sweep(State &s, const void *U, uint32_t *n_partials) {
         const uint32_t blocks = (s.V + 127) / 128;
-        k_gauss_sweep<D, T, false><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.E_alt,
-                                                                  (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
-                                                                  s.block_order);
+        // rows whole inside the warps (L divides 32, every lane a site): the variant that takes the
+        // direction-0 neighbour's step by shuffle
+        const bool share0 = (kTile % s.L == 0) && (s.V % kTile == 0);
+        if (share0)
+            k_gauss_sweep<D, T, false, true><<<blocks, 128, 0, s.stream>>>(
+                (const V2<T> *)U, (const T *)s.E, (T *)s.E_alt, (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
+                s.block_order);
+        else
+            k_gauss_sweep<D, T, false><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.E_alt,
+                                                                      (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
+                                                                      s.block_order);
         *n_partials = blocks;
         return cudaGetLastError();
     }

@@ -926,13 +926,17 @@ __global__ void __launch_bounds__(128) k_md_update(const V2<T> *__restrict__ Uin
 // plus the residual partials of G'.  E and G are double-buffered (a thread reads its
 // neighbours' old values while they are being replaced).  U is read once per sweep instead
 // of twice (Gauss law, then step) and the sweep needs one launch instead of two.
-template <int D, typename T, bool COMP>
+template <int D, typename T, bool COMP, bool SHARE0 = false>
 __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                              T *__restrict__ Eout, const T *__restrict__ Gin, T *__restrict__ Gout,
                                              const Geo<D> &g, uint32_t site, size_t elo) {
     {
         uint32_t c[D];
         site_coords(g, site, c);
+        // SHARE0 (the caller has checked that L divides 32 and every lane of a warp holds a site, so
+        // the rows lie whole inside the warps): the step of link (x - 0, 0) is the own step of the
+        // lane holding x - 0, taken by a shuffle instead of recomputed -- the same arithmetic on the
+        // same inputs, so the same bits
         mat3<T> gx, gnew;
         herm_load(Gin, site, gx);
         T gxc[8];
@@ -963,18 +967,26 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
             }
             {
                 const uint32_t xm = bwd(g, site, c[mu], mu);
-                mat3<T> w, gm, t, wm;
+                mat3<T> w, t, wm;
                 load_link<T>(U, tix(xm, D * 9, mu * 9), w);
-                herm_load(Gin, xm, gm);
-                T gmc[8];
-                two_re_tr_generators(gm, gmc);
-                const size_t ei = tix(xm, D * 8, mu * 8);
-                load_efield<T>(Ein, ei, e);
-                if (COMP) load_efield<T>(Ein + elo, ei, el);
-                else
+                if (!COMP && SHARE0 && mu == 0) {
+                    const unsigned lane = site & (kTile - 1);
+                    const unsigned src = c[0] > 0 ? lane - 1 : lane + g.L - 1;
 #pragma unroll
-                    for (int a = 0; a < 8; ++a) el[a] = T(0);
-                projection_step<T, COMP>(w, gm, gmc, gx, e, el);
+                    for (int a = 0; a < 8; ++a) e[a] = __shfl_sync(0xffffffffu, e[a], src);
+                } else {
+                    mat3<T> gm;
+                    herm_load(Gin, xm, gm);
+                    T gmc[8];
+                    two_re_tr_generators(gm, gmc);
+                    const size_t ei = tix(xm, D * 8, mu * 8);
+                    load_efield<T>(Ein, ei, e);
+                    if (COMP) load_efield<T>(Ein + elo, ei, el);
+                    else
+#pragma unroll
+                        for (int a = 0; a < 8; ++a) el[a] = T(0);
+                    projection_step<T, COMP>(w, gm, gmc, gx, e, el);
+                }
                 adj_mul<T>(e, w, t);
                 mul_an_herm(w, t, wm); // U^dag E' U is Hermitian
 #pragma unroll
@@ -993,7 +1005,7 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
         return (double)(fabs(sum) * T(0.5));
     }
 }
-template <int D, typename T, bool COMP>
+template <int D, typename T, bool COMP, bool SHARE0 = false>
 __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                                      T *__restrict__ Eout, const T *__restrict__ Gin,
                                                      T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial,
@@ -1002,7 +1014,7 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const 
     const uint32_t site = blk * blockDim.x + threadIdx.x;
     double r[1] = {0.0};
     if (site < g.V)
-        r[0] = sweep_site<D, T, COMP>(U, Ein, Eout, Gin, Gout, g, site, (size_t)tiles_of(g.V) * D * 8 * kTile);
+        r[0] = sweep_site<D, T, COMP, SHARE0>(U, Ein, Eout, Gin, Gout, g, site, (size_t)tiles_of(g.V) * D * 8 * kTile);
     block_reduce_store<1>(r, partial, blk, gridDim.x);
 }
 

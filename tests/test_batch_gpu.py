@@ -190,12 +190,14 @@ def test_eager_kernel_profile_counts_every_launch(lqgpu_mod):
         b.profile_enable(False)
 
 
-@pytest.mark.parametrize("dim,L", [(2, 32), (3, 32), (4, 32), (4, 48)])
+@pytest.mark.parametrize("dim,L", [(2, 32), (3, 32), (4, 32), (4, 48), (2, 16), (3, 8), (4, 8)])
 def test_lone_state_at_L32_equals_batched_ensemble(lqgpu_mod, dim, L):
     """the headline's side length: a lone mixed state and the same lattice as a one-ensemble batch
     (the batch's persistent kernels over a chunk table) give the same accept decisions, projection
     steps and links, bitwise.  At 48^4 the lone state's MD and sweep kernels visit their blocks in
-    strips (block_order.hpp) while the batch's run in site order."""
+    strips (block_order.hpp) while the batch's run in site order; where L divides 32 (32, 16, 8: one
+    or several lattice rows per warp) the lone state's sweep takes the direction-0 neighbour's step
+    by shuffle while the batch's recomputes it."""
     G = lqgpu_mod
     with G.Batch(dim, [L], [1000.0], [2.0], G.PRECISION_MIXED) as b:
         b.set_links_random(LINK_SEED)

@@ -454,12 +454,25 @@ def run_ours(args):
     s.set_stream(stream.cuda_stream)
     s.set_projection_graph(args.projection == "graph")
     s.set_links_random(1 + rank)
+    # inside the timed region only the MD launches carry CUDA events (the roofline's kernel time);
+    # the other classes run without them
     s.profile_enable(True)
+    s.profile_classes(["md"])
     ms, wall, prof, res, clocks = timed_trajectories(s, args.warmup, args.steps, 77 + rank, sample_clocks=True)
     ms_max = max_over_ranks(ms)
     value = replica_value(n_links * nmd * args.steps, ms, max_over_ranks, sum_over_ranks)
-    launches = sum(v[0] for v in prof.values())
     md_launches, md_ms = prof["md"]
+    # every class timed on a few more trajectories of the same state: the kernel breakdown and the
+    # launches of a trajectory (the same launches every trajectory but for its projection's sweeps)
+    s.profile_classes(None)
+    k_all = 3
+    _, _, prof_all, res_all, _ = timed_trajectories(s, 0, k_all, 177 + rank)
+    s.profile_enable(False)
+    sweeps_all = sum(r["gauss_steps"] for r in res_all)
+    sweeps_timed = sum(r["gauss_steps"] for r in res)
+    per_sweep = prof_all["gauss_sweep"][0] / max(1, sweeps_all)  # sweep-loop launches per sweep (graph nodes)
+    launches_fixed = (sum(v[0] for v in prof_all.values()) - prof_all["gauss_sweep"][0]) / k_all
+    launches = int(round(launches_fixed * args.steps + per_sweep * sweeps_timed))
     md_bytes = algorithmic_md_bytes(n_links, nmd, real_bytes, prec == lqgpu.PRECISION_MIXED) * args.steps
     peak, peak_kind = measured_peaks()
     achieved = md_bytes / (md_ms / 1000.0) / 1e9 if md_ms > 0 else 0.0
@@ -520,11 +533,14 @@ def run_ours(args):
         s64.set_stream(stream.cuda_stream)
         s64.set_links_random(1 + rank)
         s64.profile_enable(True)
+        s64.profile_classes(["md"])
         ms64, _, prof64, res64, _ = timed_trajectories(s64, 1, args.fp64_steps, 77 + rank)
         # the projection runs as one graph launch: its kernels' FP64 rates come from one more
         # trajectory with the host-driven loop, which the profile sees kernel by kernel
+        s64.profile_classes(None)
         s64.set_projection_graph(False)
         _, _, prof64k, _, _ = timed_trajectories(s64, 0, 1, 78 + rank)
+        s64.profile_enable(False)
         ms64 = max_over_ranks(ms64)
         v64 = sum_over_ranks(n_links * nmd * args.fp64_steps) / (ms64 / 1000.0)
         md64_n, md64_ms = prof64["md"]
@@ -532,7 +548,7 @@ def run_ours(args):
                 "headline_over_fp64": value / v64,
                 "md_kernel_ms": md64_ms / max(1, md64_n),
                 "gauss_steps": [r["gauss_steps"] for r in res64],
-                "kernel_ms": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof64.items()},
+                "kernel_ms": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof64k.items()},
                 "roofline_fp64": fp64_roofline(prof64k, n_links, L ** dim, nmd, 1,
                                                lqgpu.fma_peak(lqgpu.PRECISION_F64))}
         other = lqgpu.PRECISION_F32 if prec == lqgpu.PRECISION_MIXED else lqgpu.PRECISION_MIXED
@@ -540,7 +556,9 @@ def run_ours(args):
         so.set_stream(stream.cuda_stream)
         so.set_links_random(1 + rank)
         so.profile_enable(True)
+        so.profile_classes(["md"])
         mso, _, profo, reso, _ = timed_trajectories(so, 1, max(2, args.fp64_steps), 77 + rank)
+        so.profile_enable(False)
         mso = max_over_ranks(mso)
         vo = sum_over_ranks(n_links * nmd * max(2, args.fp64_steps)) / (mso / 1000.0)
         f32 = {"precision": "f32" if other == lqgpu.PRECISION_F32 else "mixed", "value": vo, "unit": UNIT,
@@ -625,8 +643,13 @@ def run_ours(args):
                          "traffic_source": "ncu dram bytes per link at 28^4 scaled to 32^4",
                          "algorithmic_bytes_per_link": 52 * real_bytes,
                          "md_launch_ms": md_ms / max(1, md_launches)},
-            "kernel_ms": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+            "kernel_ms": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof_all.items()},
+            "kernel_ms_pass": "%d further trajectories of the same state with every launch timed (in the timed "
+                              "region only the MD launches carry events)" % k_all,
             "gpu_launches": launches,
+            "gpu_launches_count": "the launches of each trajectory of the timed region: per trajectory those of the "
+                                  "fully timed pass, the projection's launches per sweep times the sweeps each timed "
+                                  "trajectory made",
             "gauss_steps": gauss_steps, "acceptance": acc_rate, "plaquette": plaq_mixed.real / 3.0,
             "wall_ms_per_step": 1000.0 * wall / args.steps,
             "clocks": clocks, "e2e": e2e, "fp64": fp64, "other_precision": f32, "accuracy": accuracy,

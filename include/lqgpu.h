@@ -299,15 +299,18 @@ int lq_hmc_trajectory(lq_state *s, double dt, int n_steps, uint64_t seed, uint64
  * reference counterpart: the reference has no tracing).  While enabled, every launch of
  * the state is bracketed by an event pair; totals accumulate at each synchronisation. */
 enum lq_kernel_class {
-    LQ_KERNEL_MD = 0,         /* fused force/kick/drift (k_md) */
-    LQ_KERNEL_GAUSS = 1,       /* Gauss law G(x) + residual partials (k_gauss) */
-    LQ_KERNEL_GAUSS_SWEEP = 2, /* projection sweep fused with the next Gauss law (k_gauss_sweep) */
+    LQ_KERNEL_MD = 0,         /* the MD step: fused force/kick/drift (k_md_site; FP64 k_md_plaq + k_md_update) */
+    LQ_KERNEL_GAUSS = 1,       /* Gauss law G(x) + residual partials (k_gauss; FP64 projection k_gauss_adj) */
+    LQ_KERNEL_GAUSS_SWEEP = 2, /* projection sweep (k_gauss_sweep; FP64 k_gauss_step_adj; a projection graph) */
     LQ_KERNEL_PLAQUETTE = 3,  /* plaquette / hamiltonian_links partials (k_plaquette) */
     LQ_KERNEL_REDUCE = 4,     /* sum of squares and final reductions */
     LQ_KERNEL_OTHER = 5,      /* layout conversion, initialisation, reprojection */
     LQ_KERNEL_CLASSES = 6
 };
 int lq_profile_enable(lq_state *s, int on);
+/* Restrict the profile to the classes whose bit is set in mask (bit k: class k; all by default):
+ * launches of the other classes run without events, so timing one class costs the others nothing. */
+int lq_profile_classes(lq_state *s, unsigned mask);
 /* Measured multiply-add peak of the current device (no reference counterpart): long chains of
  * independent multiply-adds in LQ_PRECISION_F64 or LQ_PRECISION_F32 on every SM, timed with CUDA
  * events at the clocks the device runs at; *flops_per_s counts 2 FLOP per multiply-add.  The

@@ -45,7 +45,7 @@ int cuda_fail(cudaError_t e, const char *what, int line) {
 
 #define LQ_LAUNCH(st, cls, call)                                                                                       \
     do {                                                                                                               \
-        const int _slot = prof_begin(st);                                                                              \
+        const int _slot = prof_begin(st, cls);                                                                         \
         cudaError_t _e = (call);                                                                                       \
         prof_end(st, _slot, cls);                                                                                      \
         if (_e != cudaSuccess) return cuda_fail(_e, #call, __LINE__);                                                  \
@@ -76,9 +76,9 @@ cudaError_t sync_stream(State &s) {
     if (e == cudaSuccess) prof_flush(s);
     return e;
 }
-int prof_begin(State &s) {
+int prof_begin(State &s, int cls) {
     lq::Prof *p = s.prof;
-    if (!p) return -1;
+    if (!p || !((s.prof_mask >> cls) & 1u)) return -1;
     if (p->n == lq::kProfPool) {
         if (cudaStreamSynchronize(s.stream) != cudaSuccess) return -1;
         prof_flush(s);
@@ -351,7 +351,7 @@ int project_gauss_graph(State &s, int max_steps, int *steps_done) {
         }
         s.proj[s.n_proj++] = {U, s.E, s.G, max_steps, exec};
     }
-    const int slot = prof_begin(s);
+    const int slot = prof_begin(s, LQ_KERNEL_GAUSS_SWEEP);
     const cudaError_t e = cudaGraphLaunch(exec, s.stream);
     prof_end(s, slot, LQ_KERNEL_GAUSS_SWEEP);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch (projection)", __LINE__);
@@ -1402,6 +1402,12 @@ int lq_profile_enable(lq_state *s, int on) {
     } else if (!on) {
         prof_free(*s);
     }
+    return LQ_OK;
+}
+
+int lq_profile_classes(lq_state *s, unsigned mask) {
+    LQ_CHECK_STATE(s);
+    s->prof_mask = mask;
     return LQ_OK;
 }
 

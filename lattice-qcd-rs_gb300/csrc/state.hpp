@@ -92,7 +92,8 @@ struct State {
     double hu = 0.0;
 
     const Ops *ops = nullptr;
-    Prof *prof = nullptr; // non-null while profiling is enabled
+    Prof *prof = nullptr;       // non-null while profiling is enabled
+    unsigned prof_mask = ~0u;   // the kernel classes the profile times (lq_profile_classes)
     // launch order of the per-site stencil kernels' blocks (block_order.hpp)
     BlockOrder block_order = {0, 1, 1, 1};
 

@@ -92,6 +92,7 @@ SIGNATURES = {
     "lq_magnetic_field": (_i32, [_vp, _dp, _sz]),
     "lq_leapfrog_adjoint": (_i32, [_vp, _f64, _i32, _i32, _dp, _dp, _dp, _sz, _dp, _sz, _szp]),
     "lq_profile_enable": (_i32, [_vp, _i32]),
+    "lq_profile_classes": (_i32, [_vp, ctypes.c_uint]),
     "lq_profile_read": (_i32, [_vp, _i32, _llp, _dp, _i32]),
     "lq_fma_peak": (_i32, [_i32, _dp]),
     "lq_batch_create": (_i32, [_i32, _i32, _ip, _dp, _dp, _i32, ctypes.POINTER(_vp)]),
@@ -389,6 +390,11 @@ class State:
 
     def profile_enable(self, on=True):
         _check(load().lq_profile_enable(self._h, 1 if on else 0), "lq_profile_enable")
+
+    def profile_classes(self, names=None):
+        """time only these kernel classes (names from KERNEL_CLASSES; None: all)"""
+        mask = 0xFFFFFFFF if names is None else sum(1 << self.KERNEL_CLASSES.index(n) for n in names)
+        _check(load().lq_profile_classes(self._h, mask), "lq_profile_classes")
 
     def profile_read(self, reset=False):
         """{class: (launches, total_ms)} since the last reset."""

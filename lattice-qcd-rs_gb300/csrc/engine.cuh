@@ -9,6 +9,10 @@
 #include "state.hpp"
 #include "sweeps.cuh"
 
+#ifndef LQ_SWEEP_SHARE1
+#define LQ_SWEEP_SHARE1 1
+#endif
+
 namespace lq {
 
 template <int D, typename T, bool COMP> struct Engine {
@@ -131,7 +135,12 @@ template <int D, typename T, bool COMP> struct Engine {
         // rows whole inside the warps (L divides 32, every lane a site): the variant that takes the
         // direction-0 neighbour's step by shuffle
         const bool share0 = (kTile % s.L == 0) && (s.V % kTile == 0);
-        if (share0)
+        const bool share1 = LQ_SWEEP_SHARE1 && s.L == kTile && s.V % 128 == 0 && !s.block_order.on;
+        if (share1)
+            k_gauss_sweep<D, T, false, true, true><<<blocks, 128, 0, s.stream>>>(
+                (const V2<T> *)U, (const T *)s.E, (T *)s.E_alt, (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
+                s.block_order);
+        else if (share0)
             k_gauss_sweep<D, T, false, true><<<blocks, 128, 0, s.stream>>>(
                 (const V2<T> *)U, (const T *)s.E, (T *)s.E_alt, (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
                 s.block_order);

@@ -926,17 +926,20 @@ __global__ void __launch_bounds__(128) k_md_update(const V2<T> *__restrict__ Uin
 // plus the residual partials of G'.  E and G are double-buffered (a thread reads its
 // neighbours' old values while they are being replaced).  U is read once per sweep instead
 // of twice (Gauss law, then step) and the sweep needs one launch instead of two.
-template <int D, typename T, bool COMP, bool SHARE0 = false>
+template <int D, typename T, bool COMP, bool SHARE0 = false, bool SHARE1 = false>
 __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                              T *__restrict__ Eout, const T *__restrict__ Gin, T *__restrict__ Gout,
-                                             const Geo<D> &g, uint32_t site, size_t elo) {
+                                             const Geo<D> &g, uint32_t site, size_t elo, T (*s1)[128] = nullptr) {
     {
         uint32_t c[D];
         site_coords(g, site, c);
         // SHARE0 (the caller has checked that L divides 32 and every lane of a warp holds a site, so
         // the rows lie whole inside the warps): the step of link (x - 0, 0) is the own step of the
         // lane holding x - 0, taken by a shuffle instead of recomputed -- the same arithmetic on the
-        // same inputs, so the same bits
+        // same inputs, so the same bits.  SHARE1 (L = 32 and every thread of a block a site, so the
+        // block's four warps are four consecutive rows): warps 1..3 take the step of link
+        // (x - 1, 1) from the warp before theirs through shared memory (s1, after a barrier every
+        // thread of the block reaches); warp 0 recomputes it
         mat3<T> gx, gnew;
         herm_load(Gin, site, gx);
         T gxc[8];
@@ -958,6 +961,11 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
                 projection_step<T, COMP>(u, gx, gxc, gp, e, el);
                 store_efield<T>(Eout, ei, e);
                 if (COMP) store_efield<T>(Eout + elo, ei, el);
+                if (SHARE1 && mu == 1) {
+#pragma unroll
+                    for (int a = 0; a < 8; ++a) s1[a][threadIdx.x] = e[a];
+                    __syncthreads();
+                }
                 adjoint_to_matrix<T>(e, em);
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
@@ -974,6 +982,9 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
                     const unsigned src = c[0] > 0 ? lane - 1 : lane + g.L - 1;
 #pragma unroll
                     for (int a = 0; a < 8; ++a) e[a] = __shfl_sync(0xffffffffu, e[a], src);
+                } else if (!COMP && SHARE1 && mu == 1 && threadIdx.x >= kTile) {
+#pragma unroll
+                    for (int a = 0; a < 8; ++a) e[a] = s1[a][threadIdx.x - kTile];
                 } else {
                     mat3<T> gm;
                     herm_load(Gin, xm, gm);
@@ -1005,16 +1016,18 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
         return (double)(fabs(sum) * T(0.5));
     }
 }
-template <int D, typename T, bool COMP, bool SHARE0 = false>
+template <int D, typename T, bool COMP, bool SHARE0 = false, bool SHARE1 = false>
 __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                                      T *__restrict__ Eout, const T *__restrict__ Gin,
                                                      T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial,
                                                      BlockOrder bo) {
+    __shared__ T s1[SHARE1 ? 8 : 1][128];
     const uint32_t blk = block_at(bo, blockIdx.x); // the residual partial keeps its site-order slot
     const uint32_t site = blk * blockDim.x + threadIdx.x;
     double r[1] = {0.0};
     if (site < g.V)
-        r[0] = sweep_site<D, T, COMP, SHARE0>(U, Ein, Eout, Gin, Gout, g, site, (size_t)tiles_of(g.V) * D * 8 * kTile);
+        r[0] = sweep_site<D, T, COMP, SHARE0, SHARE1>(U, Ein, Eout, Gin, Gout, g, site,
+                                                      (size_t)tiles_of(g.V) * D * 8 * kTile, s1);
     block_reduce_store<1>(r, partial, blk, gridDim.x);
 }
 

@@ -60,9 +60,8 @@ template <int D, typename T, bool COMP> struct Engine {
         k_efield_to_aos<D, T, COMP><<<link_blocks(s, 128), 128, 0, s.stream>>>((const T *)E, d_aos, s.V, elo(s));
         return cudaGetLastError();
     }
-    // out <- scale * Im Tr(T^a U_mu(x) Sigma_mu(x)) on every link (out zeroed by the caller)
-    // launch shape of k_md: 128 sites of one direction per block, directions fastest (a shape of
-    // 32 sites x D directions per block measured 13% slower at 32^4)
+    // launch shape of the per-link kernels (k_md, k_md_update): 128 sites of one direction per block,
+    // directions fastest (a shape of 32 sites x D directions per block measured 13% slower at 32^4)
     static dim3 md_grid_k(const State &s) { return dim3(((s.V + 127) / 128) * D, 1, 1); }
     static unsigned md_block_k() { return 128; }
     // The FP64 state: k_md_plaq + k_md_update.  Otherwise one thread per site (k_md_site) or per link
@@ -81,6 +80,7 @@ template <int D, typename T, bool COMP> struct Engine {
                 (const V2<T> *)Uin, (V2<T> *)Uout, (const T *)Ein, (T *)Eout, geo(s), k1, k2, drift);
         }
     }
+    // out <- scale * Im Tr(T^a U_mu(x) Sigma_mu(x)) on every link (out zeroed by the caller)
     static cudaError_t force(State &s, const void *U, void *out, double scale) {
         // kick only: the output links are never written (null)
         launch_md<MD_KICK>(s, U, nullptr, out, out, T(0), (T)scale, T(0));

@@ -9,7 +9,10 @@
 //              with COMP the lo parts follow as a second array of the same shape
 //   efield E : T, P = D*8 planes, planes mu*8 .. mu*8+7 hold e^a of E_mu, packed per site into
 //              16-byte vectors (efield_off / load_efield) (+ lo array with COMP)
-//   gauss  G : T, P = 9 planes, Hermitian G(x): real diagonal + upper off-diagonal
+//   gauss  G : T, P = 9 planes, Hermitian G(x): real diagonal + upper off-diagonal; in the FP64
+//              projection 10 planes, the 9 components of G and a pad, packed like E
+//   scratch  : FP64 only, D*82 planes per site: the projection's per-link transport tables, and
+//              between projections the MD step's per-link force parts
 // Sites are linearised x_0 fastest as in the reference (src/lattice.rs:909-916), so the
 // +-mu neighbour of a site is +-L^mu with periodic wrap.  Arrays are padded to whole tiles;
 // padded sites are never written by the kernels and stay zero.

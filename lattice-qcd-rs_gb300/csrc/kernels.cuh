@@ -970,17 +970,15 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
                     __syncthreads();
                 }
                 adjoint_to_matrix<T>(e, em);
-                // G' is Hermitian: its diagonal and upper triangle are kept
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
-                    if (k == 3 || k == 6 || k == 7) continue;
                     gnew.e[k].re += em.e[k].re;
-                    if (k != 0 && k != 4 && k != 8) gnew.e[k].im += em.e[k].im;
+                    gnew.e[k].im += em.e[k].im;
                 }
             }
             {
                 const uint32_t xm = bwd(g, site, c[mu], mu);
-                mat3<T> w, t;
+                mat3<T> w, t, wm;
                 load_link<T>(U, tix(xm, D * 9, mu * 9), w);
                 if (!COMP && SHARE0 && mu == 0) {
                     const unsigned lane = site & (kTile - 1);
@@ -1004,24 +1002,17 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
                     projection_step<T, COMP>(w, gm, gmc, gx, e, el);
                 }
                 adj_mul<T>(e, w, t);
-                {
-                    // G' -= U^dag E' U (Hermitian): the diagonal and upper triangle.  Subtracting
-                    // the finished product measured faster at 32^4 than chains that start from G'
-                    // (0.1315 against 0.1335 ms per sweep), slower at 128^3 (0.212 against 0.200)
-                    mat3<T> wm;
-                    mul_an_herm(w, t, wm);
+                mul_an_herm(w, t, wm); // U^dag E' U is Hermitian
 #pragma unroll
-                    for (int k = 0; k < 9; ++k) {
-                        if (k == 3 || k == 6 || k == 7) continue;
-                        gnew.e[k].re -= wm.e[k].re;
-                        if (k != 0 && k != 4 && k != 8) gnew.e[k].im -= wm.e[k].im;
-                    }
+                for (int k = 0; k < 9; ++k) {
+                    gnew.e[k].re -= wm.e[k].re;
+                    gnew.e[k].im -= wm.e[k].im;
                 }
             }
         }
         herm_store(Gout, site, gnew);
         T gc[8];
-        two_re_tr_generators_upper(gnew, gc);
+        two_re_tr_generators(gnew, gc);
         T sum = T(0);
 #pragma unroll
         for (int a = 0; a < 8; ++a) sum += gc[a];

@@ -191,18 +191,6 @@ template <typename T> __device__ __forceinline__ void mul_na_herm(const mat3<T> 
 }
 
 // r = a^dagger * b for a product known to be Hermitian (U^dag E U): as mul_na_herm
-// out^a = 2 Re Tr(T^a X) for a Hermitian X given by its diagonal and upper triangle
-template <typename T> __device__ __forceinline__ void two_re_tr_generators_upper(const mat3<T> &x, T *out) {
-    out[0] = T(2) * x.e[1].re;
-    out[1] = T(-2) * x.e[1].im;
-    out[2] = x.e[0].re - x.e[4].re;
-    out[3] = T(2) * x.e[2].re;
-    out[4] = T(-2) * x.e[2].im;
-    out[5] = T(2) * x.e[5].re;
-    out[6] = T(-2) * x.e[5].im;
-    out[7] = T(2.0 * kOneOver2Sqrt3) * (x.e[0].re + x.e[4].re) + T(2.0 * kMinusOneOverSqrt3) * x.e[8].re;
-}
-
 template <typename T> __device__ __forceinline__ void mul_an_herm(const mat3<T> &a, const mat3<T> &b, mat3<T> &r) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) {

@@ -14,7 +14,7 @@ precision : D = 4, 32^4, beta in {0.5, 1, 2, 4}, random_su3 start (seed 1), 20 l
             standard deviations near 1, i.e. beta = 0.5), the beta records the failure.
 scale     : D = 4 at 24^4, 32^4, 48^4, 64^4 and D = 3 at 128^3, 256^3, beta 2, seed 4, 20 steps
             dt 0.005: link-updates/s of FP64 and mixed (device time of K trajectories), the
-            k_md kernel's achieved HBM bandwidth, and the Delta H / plaquette error of mixed.
+            MD kernel's (k_md_site) achieved HBM bandwidth, and the Delta H / plaquette error of mixed.
 
 batch     : 64 ensembles of uneven side length and beta advanced together (one launch per kernel
             over every ensemble, a CUDA graph per trajectory), against the same ensembles run

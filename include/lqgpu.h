@@ -308,6 +308,13 @@ enum lq_kernel_class {
     LQ_KERNEL_CLASSES = 6
 };
 int lq_profile_enable(lq_state *s, int on);
+/* Index checks, no reference counterpart (a stand-in for a memory checker): in a library built with
+ * -DLQ_BOUNDS_CHECK=1 the kernels compare every site
+ * index they form (neighbours, coordinates) and every tile plane with its bound, count a bad one
+ * instead of using it (the access goes to index 0) and keep the first.  *enabled: 1 in such a build,
+ * 0 otherwise (then *violations is 0 and no device call is made).  *first_bad: the first bad index
+ * + 1 (0: none); a plane index reads (planes << 32) | plane.  reset != 0 clears the counters. */
+int lq_bounds_check(int *enabled, unsigned long long *violations, unsigned long long *first_bad, int reset);
 /* Restrict the profile to the classes whose bit is set in mask (bit k: class k; all by default):
  * launches of the other classes run without events, so timing one class costs the others nothing. */
 int lq_profile_classes(lq_state *s, unsigned mask);

@@ -58,7 +58,7 @@ template <int D> __device__ __forceinline__ uint32_t div_by_L(const Geo<D> &g, u
 
 // coordinates of a site, c[i] = (site / L^i) % L, one division by L per direction
 template <int D> __device__ __forceinline__ void site_coords(const Geo<D> &g, uint32_t site, uint32_t *c) {
-    uint32_t r = site;
+    uint32_t r = checked_site(site, g.V);
 #pragma unroll
     for (int i = 0; i < D; ++i) {
         const uint32_t q = div_by_L(g, r);
@@ -69,11 +69,11 @@ template <int D> __device__ __forceinline__ void site_coords(const Geo<D> &g, ui
 // neighbour of `site` (whose coordinate along mu is cmu) in +mu / -mu, periodic
 template <int D>
 __device__ __forceinline__ uint32_t fwd(const Geo<D> &g, uint32_t site, uint32_t cmu, int mu) {
-    return (cmu == g.L - 1) ? site - (g.L - 1) * g.stride[mu] : site + g.stride[mu];
+    return checked_site((cmu == g.L - 1) ? site - (g.L - 1) * g.stride[mu] : site + g.stride[mu], g.V);
 }
 template <int D>
 __device__ __forceinline__ uint32_t bwd(const Geo<D> &g, uint32_t site, uint32_t cmu, int mu) {
-    return (cmu == 0) ? site + (g.L - 1) * g.stride[mu] : site - g.stride[mu];
+    return checked_site((cmu == 0) ? site + (g.L - 1) * g.stride[mu] : site - g.stride[mu], g.V);
 }
 
 template <typename T> using V2 = typename vec2_t<T>::type;

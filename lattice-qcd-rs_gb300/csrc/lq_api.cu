@@ -10,6 +10,7 @@
 #include <new>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "kernels.cuh"
 #include "lqgpu.h"
@@ -21,6 +22,20 @@ using lq::State;
 #ifndef LQ_BLOCK_REUSE_SITES
 #define LQ_BLOCK_REUSE_SITES 32768
 #endif
+
+namespace lq {
+namespace {
+using BoundsReader = int (*)(unsigned long long *, unsigned long long *, int);
+std::vector<BoundsReader> &bounds_readers() {
+    static std::vector<BoundsReader> r; // filled during static initialisation of the library
+    return r;
+}
+} // namespace
+int register_bounds_reader(BoundsReader read) {
+    bounds_readers().push_back(read);
+    return 0;
+}
+} // namespace lq
 
 namespace {
 
@@ -1402,6 +1417,18 @@ int lq_profile_enable(lq_state *s, int on) {
     } else if (!on) {
         prof_free(*s);
     }
+    return LQ_OK;
+}
+
+int lq_bounds_check(int *enabled, unsigned long long *violations, unsigned long long *first_bad, int reset) {
+    if (enabled) *enabled = LQ_BOUNDS_CHECK;
+    unsigned long long n = 0, first = 0;
+    for (lq::BoundsReader read : lq::bounds_readers()) {
+        const int e = read(&n, &first, reset);
+        if (e) return cuda_fail((cudaError_t)e, "reading the index-check counters", __LINE__);
+    }
+    if (violations) *violations = n;
+    if (first_bad) *first_bad = first;
     return LQ_OK;
 }
 

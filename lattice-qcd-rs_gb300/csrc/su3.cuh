@@ -9,7 +9,51 @@
 
 #include <type_traits>
 
+// Index checks (builds with -DLQ_BOUNDS_CHECK=1, the stand-in for a memory checker): the site and
+// plane indices the kernels form (neighbours, coordinates, tile planes) are compared with their
+// bounds; a bad one is counted in this translation unit's g_bounds, replaced by 0 so that the access
+// stays inside the array, and reported through lq_bounds_check.  Off by default: no cost.
+#ifndef LQ_BOUNDS_CHECK
+#define LQ_BOUNDS_CHECK 0
+#endif
+
 namespace lq {
+
+// host side: every translation unit of a checked build registers the reader of its own counters
+// (lq_api.cu keeps the list)
+int register_bounds_reader(int (*read)(unsigned long long *count, unsigned long long *first, int reset));
+#if LQ_BOUNDS_CHECK
+// [0] bad indices seen, [1] the first one (value + 1; plane indices as (nplanes << 32) | plane)
+static __device__ unsigned long long g_bounds[2];
+__device__ __forceinline__ void bounds_fail(unsigned long long v) {
+    if (atomicAdd(&g_bounds[0], 1ull) == 0ull) g_bounds[1] = v + 1ull;
+}
+static int read_bounds(unsigned long long *count, unsigned long long *first, int reset) {
+    unsigned long long h[2] = {0ull, 0ull};
+    cudaError_t e = cudaMemcpyFromSymbol(h, g_bounds, sizeof(h));
+    if (e == cudaSuccess && reset) {
+        const unsigned long long z[2] = {0ull, 0ull};
+        e = cudaMemcpyToSymbol(g_bounds, z, sizeof(z));
+    }
+    if (e != cudaSuccess) return (int)e;
+    *count += h[0];
+    if (h[0] && !*first) *first = h[1];
+    return 0;
+}
+[[maybe_unused]] static const int g_bounds_registered = register_bounds_reader(read_bounds);
+#endif
+// site index < n, else counted (checked builds) and replaced by 0
+__device__ __forceinline__ uint32_t checked_site(uint32_t site, uint32_t n) {
+#if LQ_BOUNDS_CHECK
+    if (site >= n) {
+        bounds_fail(site);
+        return 0u;
+    }
+#else
+    (void)n;
+#endif
+    return site;
+}
 
 template <typename T> struct cpx {
     T re, im;
@@ -507,6 +551,12 @@ __device__ __forceinline__ void orthonormalize_d(double (&re)[9], double (&im)[9
 // one contiguous segment.
 constexpr int kTile = 32;
 __host__ __device__ __forceinline__ size_t tix(uint32_t site, int nplanes, int plane) {
+#if LQ_BOUNDS_CHECK && defined(__CUDA_ARCH__)
+    if (plane < 0 || plane >= nplanes) {
+        bounds_fail(((unsigned long long)(uint32_t)nplanes << 32) | (uint32_t)plane);
+        plane = 0;
+    }
+#endif
     return ((size_t)(site >> 5) * nplanes + plane) * kTile + (site & 31);
 }
 __host__ __device__ __forceinline__ uint32_t tiles_of(uint32_t V) { return (V + kTile - 1) / kTile; }

@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(128) k_mc_sweep(V2<T> *__restrict__ U, Geo<D> 
 #pragma unroll
         for (int i = 1; i < D; ++i) q += c[i];
         c[0] = 2u * (t - row * (g.L >> 1)) + (q & 1u);
-        site = row * g.L + c[0];
+        site = checked_site(row * g.L + c[0], g.V);
     }
     if (active) {
         const size_t ulo = (size_t)tiles_of(g.V) * D * 9 * kTile;

@@ -93,6 +93,7 @@ SIGNATURES = {
     "lq_leapfrog_adjoint": (_i32, [_vp, _f64, _i32, _i32, _dp, _dp, _dp, _sz, _dp, _sz, _szp]),
     "lq_profile_enable": (_i32, [_vp, _i32]),
     "lq_profile_classes": (_i32, [_vp, ctypes.c_uint]),
+    "lq_bounds_check": (_i32, [_ip, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong), _i32]),
     "lq_profile_read": (_i32, [_vp, _i32, _llp, _dp, _i32]),
     "lq_fma_peak": (_i32, [_i32, _dp]),
     "lq_batch_create": (_i32, [_i32, _i32, _ip, _dp, _dp, _i32, ctypes.POINTER(_vp)]),
@@ -577,3 +578,13 @@ def fma_peak(precision=PRECISION_F64):
     v = ctypes.c_double()
     _check(load().lq_fma_peak(precision, ctypes.byref(v)), "lq_fma_peak")
     return v.value
+
+
+def bounds_check(reset=True):
+    """(enabled, violations, first bad index + 1) of the index checks (lq_bounds_check); enabled is
+    False unless the library was built with -DLQ_BOUNDS_CHECK=1"""
+    en = ctypes.c_int()
+    n, first = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    _check(load().lq_bounds_check(ctypes.byref(en), ctypes.byref(n), ctypes.byref(first), int(reset)),
+           "lq_bounds_check")
+    return bool(en.value), n.value, first.value

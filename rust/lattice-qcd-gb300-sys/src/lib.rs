@@ -2,7 +2,7 @@
 //! arguments, and the header's constants.  Each function returns an `lq_status` code (`LQ_OK` = 0);
 //! the safe wrappers of the `lattice-qcd-gb300` crate turn them into the reference's types and errors.
 #![allow(non_camel_case_types)]
-use std::os::raw::{c_char, c_double, c_int, c_longlong, c_uint, c_void};
+use std::os::raw::{c_char, c_double, c_int, c_longlong, c_uint, c_ulonglong, c_void};
 
 /// Device-resident HMC state (opaque)
 #[repr(C)]
@@ -127,6 +127,7 @@ extern "C" {
     pub fn lq_hmc_decide(s: *mut lq_state, accept: c_int) -> c_int;
     pub fn lq_hmc_trajectory(s: *mut lq_state, dt: c_double, n_steps: c_int, seed: u64, counter: u64, uniform: c_double, max_gauss_steps: c_int, accepted: *mut c_int, prob: *mut c_double, delta_h: *mut c_double, gauss_steps: *mut c_int) -> c_int;
     pub fn lq_profile_enable(s: *mut lq_state, on: c_int) -> c_int;
+    pub fn lq_bounds_check(enabled: *mut c_int, violations: *mut c_ulonglong, first_bad: *mut c_ulonglong, reset: c_int) -> c_int;
     pub fn lq_profile_classes(s: *mut lq_state, mask: c_uint) -> c_int;
     pub fn lq_fma_peak(precision: c_int, flops_per_s: *mut c_double) -> c_int;
     pub fn lq_profile_read(s: *mut lq_state, kernel_class: c_int, launches: *mut c_longlong, total_ms: *mut c_double, reset: c_int) -> c_int;

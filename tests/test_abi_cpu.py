@@ -47,6 +47,12 @@ def test_status_strings(lqgpu_mod):
     assert lib.lq_version() >= 100
 
 
+def test_index_checks_are_off_in_the_product_build(lqgpu_mod):
+    """the product library is built without the index checks: lq_bounds_check reports them off and
+    makes no device call (it answers on a host without a GPU)"""
+    assert lqgpu_mod.bounds_check() == (False, 0, 0)
+
+
 def test_argument_validation_precedes_device_use(lqgpu_mod):
     """LatticeCyclic::new validation order (src/lattice.rs:190-201) is checked on the host
     before any device call."""

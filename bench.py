@@ -57,7 +57,39 @@ def parse():
                     help="timed trajectories of the batched-ensembles leg, the configuration's 50 (0: skip it)")
     ap.add_argument("--batch-gap-traj", type=int, default=10,
                     help="trajectories of the batch leg's graph-gap measurement (0: skip it)")
+    ap.add_argument("--host-driver-traj", type=int, default=10,
+                    help="timed trajectories of the C++ HybridMonteCarloDiagnostic leg (0: skip it)")
     return ap.parse_args()
+
+
+def run_host_driver(args, prec):
+    """The C++ host interface's HybridMonteCarloDiagnostic (lattice-qcd-rs_gb300/host) driving a
+    device-resident state in its own process: compiled here against the in-tree library, timed by the
+    host clock.  None when the compiler or the run fails (the line says why)."""
+    import lqgpu
+
+    pkg = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lattice-qcd-rs_gb300")
+    lib_dir = os.path.dirname(lqgpu.LIB_PATH)
+    exe = os.path.join(lib_dir, "hmc_driver_timing")
+    src = os.path.join(pkg, "host", "hmc_driver_timing.cpp")
+    inc = os.path.join(os.path.dirname(pkg), "include")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", inc, "-I", os.path.join(pkg, "host"), src, "-o", exe, "-L", lib_dir,
+           "-llqgpu", "-Wl,-rpath," + lib_dir]
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+        if r.returncode != 0:
+            return {"unavailable": "g++ failed: " + r.stderr.strip()[-200:]}
+        r = subprocess.run([exe, str(args.L), str(args.host_driver_traj), "3", str(prec), str(args.md_steps),
+                            repr(args.dt), repr(args.beta)], capture_output=True, text=True, timeout=600)
+        if r.returncode != 0:
+            return {"unavailable": "run failed: " + (r.stderr or r.stdout).strip()[-200:]}
+        out = json.loads(r.stdout.strip().splitlines()[-1])
+    except (OSError, subprocess.SubprocessError, ValueError) as e:
+        return {"unavailable": "%s: %s" % (type(e).__name__, e)}
+    out["path"] = ("C++ HybridMonteCarloDiagnostic<4>::next_element per trajectory (new_random_e_state with device "
+                   "momenta keyed by the driver's Xoshiro256++, lq_hmc_propose, the host's accept draw, "
+                   "lq_hmc_decide), a separate process, host clock, D=4 %d^4 as the headline" % args.L)
+    return out
 
 
 def dist_env():
@@ -524,6 +556,12 @@ def run_ours(args):
     plaq_mixed = s.average_trace_plaquette()
     s.close()
 
+    # ---- the C++ host interface's HMC driver on the same workload (N = 1 only: its own process)
+    host_driver = None
+    if args.host_driver_traj > 0 and world == 1 and args.dim == 4:
+        torch.cuda.synchronize()
+        host_driver = run_host_driver(args, prec)
+
     # ---- FP64 leg (the plain GPU form), the plain-FP32-storage leg, and accuracy at equal inputs
     fp64 = None
     f32 = None
@@ -652,7 +690,8 @@ def run_ours(args):
                                   "trajectory made",
             "gauss_steps": gauss_steps, "acceptance": acc_rate, "plaquette": plaq_mixed.real / 3.0,
             "wall_ms_per_step": 1000.0 * wall / args.steps,
-            "clocks": clocks, "e2e": e2e, "fp64": fp64, "other_precision": f32, "accuracy": accuracy,
+            "clocks": clocks, "e2e": e2e, "host_driver": host_driver, "fp64": fp64, "other_precision": f32,
+            "accuracy": accuracy,
             "batch": batch, "cpu_baseline": cpu,
         }
         print(json.dumps(line))

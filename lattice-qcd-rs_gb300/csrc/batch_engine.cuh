@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(128) k_gauss_batch(BView<T> v, int ein, int go
 // partial row 0; ensembles whose projection has finished are skipped.  Hi parts only.
 template <int D, typename T>
 __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_sweep_batch(BView<T> v, int ein, int eout, int gin,
-                                                                          int gout) {
+                                                                          int gout, int pf) {
     for (uint32_t chunk = blockIdx.x; chunk < v.n_chunks; chunk += gridDim.x) {
         const uint2 c = v.chunks[chunk];
         if (v.run[c.x].converged) continue; // uniform over the block
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_sweep_batch(BView<
             const size_t ub = (size_t)en.tile0 * (D * 9 * kTile), eb = (size_t)en.tile0 * (D * 8 * kTile),
                          gb = (size_t)en.tile0 * (9 * kTile);
             r[0] = sweep_site<D, T, false>(sel_u(v, cur) + ub, sel_e(v, ein) + eb, sel_e(v, eout) + eb, sel_g(v, gin) + gb,
-                                           sel_g(v, gout) + gb, geo_of<D>(en), site, v.elo);
+                                           sel_g(v, gout) + gb, geo_of<D>(en), site, v.elo, nullptr, pf != 0);
         }
         block_reduce_store<1>(r, v.partial, chunk, v.n_chunks);
         __syncthreads();
@@ -448,7 +448,9 @@ template <int D, typename T, bool COMP> struct BatchEngine {
         return cudaGetLastError();
     }
     static cudaError_t sweep(Batch &b, int ein, int eout, int gin, int gout) {
-        k_sweep_batch<D, T><<<grid(b, BK_SWEEP, b.n_chunks), kChunk, 0, b.stream>>>(view(b), ein, eout, gin, gout);
+        // the single lattice's rule over the hi links of all ensembles
+        const int pf = b.total_links * 9 * sizeof(V2<T>) > kSweepPrefetchLinkBytes;
+        k_sweep_batch<D, T><<<grid(b, BK_SWEEP, b.n_chunks), kChunk, 0, b.stream>>>(view(b), ein, eout, gin, gout, pf);
         return cudaGetLastError();
     }
     static cudaError_t check(Batch &b, int steps_added, int max_steps, cudaGraphConditionalHandle h, int use_handle) {

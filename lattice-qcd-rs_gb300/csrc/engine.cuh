@@ -136,18 +136,22 @@ template <int D, typename T, bool COMP> struct Engine {
         // direction-0 neighbour's step by shuffle
         const bool share0 = (kTile % s.L == 0) && (s.V % kTile == 0);
         const bool share1 = LQ_SWEEP_SHARE1 && s.L == kTile && s.V % 128 == 0 && !s.block_order.on;
+        // L2 prefetch of each site's momenta and links once the hi links outgrow L2 (measured: 32^4
+        // 0.132 -> 0.126 ms, 48^4 0.690 -> 0.652, 128^3 0.209 -> 0.199; 24^4, whose 96 MB of hi links
+        // L2 holds, 0.0516 -> 0.0526 without the condition)
+        const int pf = (uint64_t)s.V * D * 9 * sizeof(V2<T>) > kSweepPrefetchLinkBytes;
         if (share1)
             k_gauss_sweep<D, T, false, true, true><<<blocks, 128, 0, s.stream>>>(
                 (const V2<T> *)U, (const T *)s.E, (T *)s.E_alt, (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
-                s.block_order);
+                s.block_order, pf);
         else if (share0)
             k_gauss_sweep<D, T, false, true><<<blocks, 128, 0, s.stream>>>(
                 (const V2<T> *)U, (const T *)s.E, (T *)s.E_alt, (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
-                s.block_order);
+                s.block_order, pf);
         else
             k_gauss_sweep<D, T, false><<<blocks, 128, 0, s.stream>>>((const V2<T> *)U, (const T *)s.E, (T *)s.E_alt,
                                                                       (const T *)s.G, (T *)s.G_alt, geo(s), s.partial,
-                                                                      s.block_order);
+                                                                      s.block_order, pf);
         *n_partials = blocks;
         return cudaGetLastError();
     }

@@ -110,6 +110,17 @@ template <typename T> using V2 = typename vec2_t<T>::type;
 #define LQ_MD_SITE_MIN_BLOCKS_FP64 1
 #endif
 constexpr int kMdSiteBlock = 128;
+// L2 prefetch of the site kernel's read-once update data at the start of each direction (measured at
+// 32^4: mixed 0.375 -> 0.365 ms, f32 0.310 -> 0.301 ms per kick+drift launch, bitwise the same fields)
+#ifndef LQ_MD_PREFETCH
+#define LQ_MD_PREFETCH 1
+#endif
+// The projection sweep prefetches each site's momenta and links to L2 when the hi links of the lattice
+// (of all ensembles, in a batch) exceed this many bytes: the GB300 L2 is 129 MB.
+#ifndef LQ_SWEEP_PREFETCH_LINK_BYTES
+#define LQ_SWEEP_PREFETCH_LINK_BYTES (128ull << 20)
+#endif
+constexpr uint64_t kSweepPrefetchLinkBytes = LQ_SWEEP_PREFETCH_LINK_BYTES;
 template <typename T> struct MdSite {
     static constexpr bool on = sizeof(T) == 8 ? LQ_MD_SITE_FP64 : LQ_MD_SITE_FP32;
 };
@@ -423,6 +434,24 @@ __device__ __forceinline__ void md_site(const V2<T> *__restrict__ Uin, V2<T> *__
     // memory in the FP64 and several FP32 modes)
 #pragma unroll 1
     for (int mu = 0; mu < D; ++mu) {
+#if LQ_MD_PREFETCH
+        // the update's own-link data (momenta hi and lo, the link's lo half) are read once, after the
+        // force: ask L2 for them now, so that their DRAM latency passes under the force's products
+        {
+            const size_t ui = tix(site, D * 9, mu * 9), ei = tix(site, D * 8, mu * 8);
+            constexpr int W = 16 / (int)sizeof(T); // reals per 16-byte momentum vector (load_efield)
+            const size_t lane = ei & 31;
+            const T *eq = Ein + (ei - lane) + lane * W;
+#pragma unroll
+            for (int j = 0; j < 8 / W; ++j) {
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(eq + j * W * kTile));
+                if (COMP) asm volatile("prefetch.global.L2 [%0];" ::"l"(eq + elo + j * W * kTile));
+            }
+            if (COMP)
+#pragma unroll
+                for (int k = 0; k < 9; ++k) asm volatile("prefetch.global.L2 [%0];" ::"l"(Uin + ulo + ui + k * kTile));
+        }
+#endif
         const uint32_t xpmu = fwd(g, site, c[mu], mu);
         mat3<T> umu;
         load_link<T>(Uin, tix(site, D * 9, mu * 9), umu);
@@ -932,7 +961,8 @@ __global__ void __launch_bounds__(128) k_md_update(const V2<T> *__restrict__ Uin
 template <int D, typename T, bool COMP, bool SHARE0 = false, bool SHARE1 = false>
 __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                              T *__restrict__ Eout, const T *__restrict__ Gin, T *__restrict__ Gout,
-                                             const Geo<D> &g, uint32_t site, size_t elo, T (*s1)[128] = nullptr) {
+                                             const Geo<D> &g, uint32_t site, size_t elo, T (*s1)[128] = nullptr,
+                                             bool pf = false) {
     {
         uint32_t c[D];
         site_coords(g, site, c);
@@ -944,6 +974,22 @@ __device__ __forceinline__ double sweep_site(const V2<T> *__restrict__ U, const 
         // (x - 1, 1) from the warp before theirs through shared memory (s1, after a barrier every
         // thread of the block reaches); warp 0 recomputes it
         mat3<T> gx, gnew;
+        if (pf) {
+            // this site's momenta and its links U_mu(x), mu >= 1 (the step of direction 0 loads its link
+            // at once), requested from L2 ahead of their loads
+            constexpr int W = 16 / (int)sizeof(T); // reals per 16-byte momentum vector (load_efield)
+#pragma unroll
+            for (int mu = 0; mu < D; ++mu) {
+                const size_t ei = tix(site, D * 8, mu * 8), lane = ei & 31;
+                const T *eq = Ein + (ei - lane) + lane * W;
+#pragma unroll
+                for (int j = 0; j < 8 / W; ++j) asm volatile("prefetch.global.L2 [%0];" ::"l"(eq + j * W * kTile));
+                if (mu > 0)
+#pragma unroll
+                    for (int k = 0; k < 9; ++k)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(U + tix(site, D * 9, mu * 9) + k * kTile));
+            }
+        }
         herm_load(Gin, site, gx);
         T gxc[8];
         two_re_tr_generators(gx, gxc);
@@ -1023,14 +1069,14 @@ template <int D, typename T, bool COMP, bool SHARE0 = false, bool SHARE1 = false
 __global__ void __launch_bounds__(128, MinBlocks<T>::sweep) k_gauss_sweep(const V2<T> *__restrict__ U, const T *__restrict__ Ein,
                                                      T *__restrict__ Eout, const T *__restrict__ Gin,
                                                      T *__restrict__ Gout, Geo<D> g, double *__restrict__ partial,
-                                                     BlockOrder bo) {
+                                                     BlockOrder bo, int pf) {
     __shared__ T s1[SHARE1 ? 8 : 1][128];
     const uint32_t blk = block_at(bo, blockIdx.x); // the residual partial keeps its site-order slot
     const uint32_t site = blk * blockDim.x + threadIdx.x;
     double r[1] = {0.0};
     if (site < g.V)
         r[0] = sweep_site<D, T, COMP, SHARE0, SHARE1>(U, Ein, Eout, Gin, Gout, g, site,
-                                                      (size_t)tiles_of(g.V) * D * 8 * kTile, s1);
+                                                      (size_t)tiles_of(g.V) * D * 8 * kTile, s1, pf != 0);
     block_reduce_store<1>(r, partial, blk, gridDim.x);
 }
 

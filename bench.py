@@ -243,9 +243,9 @@ def run_reference(args):
 
 # ------------------------------------------------------------------ GPU arm
 # DRAM bytes (read + write) per link of one kick+drift launch of the MD kernel (k_md_site), from one
-# ncu capture of the mixed kernel at 28^4 (1045.2 MB for 2,458,624 links); traffic scales with the
-# links of a launch, so the full-size value is this times the links.
-NCU_MD_TRAFFIC_PER_LINK = {"mixed": 1045.2e6 / 2458624}
+# ncu capture of the mixed kernel at 28^4 (1050.5 MB for 2,458,624 links, with the L2 prefetch of the
+# update data); traffic scales with the links of a launch, so the full-size value is this times the links.
+NCU_MD_TRAFFIC_PER_LINK = {"mixed": 1050.5e6 / 2458624}
 MD_KERNEL = "k_md_site (fused force + kick + drift, one thread per site)"
 
 
